@@ -1,0 +1,433 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched block-tridiagonal solve on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the production pencil batch): nsys = 65536 independent systems
+(a 256 x 256 pencil batch) of N = 256 block rows, block size m = 5, seeded
+synthetic diagonally dominant data (delta = 1.2, A_0 = C_{N-1} = 0), one line
+per system (P = 1).  A "step" is one solve of the whole batch: 16.8 M block
+rows, 11.4 GB of FP64 input (> L2, so no flush is needed between steps).
+
+Metric: block-rows/s (higher is better).  `value` times K solves on
+device-resident data with CUDA events on the launching stream; `e2e` times
+the same K solves through the public API with the inputs copied from pinned
+host memory each step and the solution copied back.
+
+Extra keys: `roofline` (algorithmic bytes 8*(3m^2+2m) per block row over the
+kernel time, against the measured HBM copy bandwidth), `fp64` (the same
+kernel against the FP64 FMA rate, which is what binds on GB300),
+`cpu_baseline` (the oracle port of the reference CPU path on the host cores,
+on a bounded sample), `variants` (the two-stage P = 16 split of the same
+batch and the long-line case m = 4, nsys = 256, N = 32768, P = 128),
+`clocks` (nvidia-smi sampled during the timed region).
+
+Under torchrun (N > 1) every rank solves its own full batch (weak scaling,
+no collective on the data path); the time is the max over ranks.
+
+`--impl reference` times the reference algorithm's CPU path (the oracle port
+of Fortran_Original/src/mod_btdma_cpu.f90; the Fortran original cannot be
+built here) on all host cores, on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+M, NSYS, NROW, NSEG, DELTA, SEED = 5, 65536, 256, 1, 1.2, 20240101
+VARIANTS = [  # name, m, nsys, nrow, nseg, delta
+    ("pencil_P16", 5, 65536, 256, 16, 1.2),
+    ("long_lines_P128", 4, 256, 32768, 128, 1.2),
+]
+
+
+def bytes_per_row(m: int, width: int = 8) -> int:
+    """Algorithmic bytes per block row: A, B, C, d read once, x written once."""
+    return width * (3 * m * m + 2 * m)
+
+
+def fp64_flops_per_row_thomas(m: int) -> float:
+    """FP64 flops per block row of the plain block Thomas recurrence:
+    R = B - A C' (2m^3), d - A y (2m^2), LU with partial pivoting
+    (2m^3/3 - m^2/2 - m/6 ... ~2m^3/3), m+1 right-hand sides (2m^2(m+1)),
+    back substitution x = y - C'x (2m^2)."""
+    return 2 * m**3 + 2 * m**2 + (2 * m**3) / 3 + 2 * m**2 * (m + 1) + 2 * m**2
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int, dev) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port of the reference CPU path, bounded sample.
+# ---------------------------------------------------------------------------
+def cpu_baseline(m: int, nrow: int, nseg: int, delta: float, target_s: float = 12.0) -> dict:
+    from oracle import oracle as O
+    from pascal_btdma_gb300 import synth
+
+    threads = O.default_threads()
+
+    def run(nsys_s):
+        w = synth.dominant(m, nsys_s, nrow, seed=SEED, delta=delta)
+        c = [O.gpu_to_cpu(m, nsys_s, nrow, k < 3, x) for k, x in enumerate(w.arrays)]
+        t0 = time.perf_counter()
+        O.solve_noncyclic_cpu(m, nsys_s, nrow, nseg, *c, nthreads=threads)
+        return time.perf_counter() - t0
+
+    n = max(threads * 8, 256)
+    dt = run(n)
+    while dt < 0.5 and n < NSYS:
+        n = min(NSYS, n * 4)
+        dt = run(n)
+    n_final = int(min(NSYS, max(n, n * target_s / max(dt, 1e-6))))
+    dt = run(n_final)
+    rows = n_final * nrow
+    return {"value": rows / dt, "unit": "block-rows/s", "cores": threads, "kind": "port",
+            "sample": f"{n_final} systems x {nrow} rows, m={m}, P={nseg}, oracle C port of mod_btdma_cpu "
+                      f"(CPU layout), {dt:.2f} s on {threads} threads"}
+
+
+# ---------------------------------------------------------------------------
+# Our arm.
+# ---------------------------------------------------------------------------
+def residual_error(a, b, c, d, x, m, nsys, nrow) -> float:
+    """max over systems of |d - M x|_inf / (|M|_inf |x|_inf + |d|_inf)."""
+    import torch
+
+    A = a.view(m, m, nrow, nsys)  # [j, i, row, sys]
+    B = b.view(m, m, nrow, nsys)
+    C = c.view(m, m, nrow, nsys)
+    X = x.view(m, nrow, nsys)     # [j, row, sys]
+    r = d.view(m, nrow, nsys) - torch.einsum("jirs,jrs->irs", B, X)
+    r[:, 1:] -= torch.einsum("jirs,jrs->irs", A[:, :, 1:], X[:, :-1])
+    r[:, :-1] -= torch.einsum("jirs,jrs->irs", C[:, :, :-1], X[:, 1:])
+    rowabs = B.abs().sum(0) + A.abs().sum(0) + C.abs().sum(0)  # [i, row, sys]
+    mnorm = rowabs.amax(dim=(0, 1))
+    num = r.abs().amax(dim=(0, 1))
+    den = mnorm * X.abs().amax(dim=(0, 1)) + d.view(m, nrow, nsys).abs().amax(dim=(0, 1))
+    return float((num / den).max())
+
+
+def make_workload(m, nsys, nrow, delta, dev, pinned=False):
+    import torch
+
+    from pascal_btdma_gb300 import synth
+
+    alloc = None
+    keep = []
+    if pinned:
+        def alloc(n):
+            t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            keep.append(t)
+            return t.numpy()
+    w = synth.dominant(m, nsys, nrow, seed=SEED, delta=delta, alloc=alloc)
+    return w, keep
+
+
+def time_device(plan, arrs, dpool, m, nsys, nrow, steps, warmup, ws, dev, solve):
+    """K solves on device-resident inputs; each step gets its own fresh RHS."""
+    import torch
+
+    a, b, c = arrs
+    stream = torch.cuda.current_stream()
+    for i in range(warmup):
+        solve(plan, a, b, c, dpool[i % len(dpool)].clone(), m, nsys, nrow)
+    work = [dpool[i % len(dpool)].clone() for i in range(steps)]
+    torch.cuda.synchronize()
+    barrier(ws)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for i in range(steps):
+        solve(plan, a, b, c, work[i], m, nsys, nrow)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = ev0.elapsed_time(ev1)
+    return ms / 1e3
+
+
+def run_ours(args):
+    import torch
+
+    import pascal_btdma_gb300 as pbt
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    peaks = load_peaks()
+    m, nsys, nrow, nseg = M, NSYS, NROW, NSEG
+
+    # Inputs: pinned host copy (for e2e) and a device copy (for `value`).
+    w, keep = make_workload(m, nsys, nrow, DELTA, dev, pinned=True)
+    hA, hB, hC, hD = (torch.from_numpy(x) for x in w.arrays)
+    a, b, c = (t.to(dev) for t in (hA, hB, hC))
+    d0 = hD.to(dev)
+    dpool = [d0]
+    plan = pbt.BtdmaGpuPlan().create(m, nsys, nrow, nseg)
+    solve = pbt.solve_noncyclic
+
+    # Accuracy of this very batch: normwise backward error of the solution,
+    # max over systems of |d - M x|_inf / (|M|_inf |x|_inf + |d|_inf), in FP64 with torch.
+    dchk = d0.clone()
+    solve(plan, a, b, c, dchk, m, nsys, nrow)
+    backward_err = residual_error(a, b, c, d0, dchk, m, nsys, nrow)
+    del dchk
+
+    # Device-resident timing (`value`) with clocks sampled during it.
+    clk = ClockSampler(local)
+    clk.start()
+    secs = time_device(plan, (a, b, c), dpool, m, nsys, nrow, args.steps, args.warmup, ws, dev, solve)
+    clocks = clk.stop()
+    secs = max_over_ranks(secs, ws, dev)
+    rows = nsys * nrow
+    value = ws * rows * args.steps / secs
+    ms_per_step = secs / args.steps * 1e3
+
+    # Kernel time for the roofline: per-launch duration with CUDA events.
+    kern_s = secs / args.steps  # one launch per solve at P = 1
+    achieved = rows * bytes_per_row(m) / kern_s / 1e9
+    fp64_rate = rows * fp64_flops_per_row_thomas(m) / kern_s / 1e12
+
+    # End to end through the public API: pinned H2D of A, B, C, D, solve, D2H of x.
+    out_h = torch.empty_like(hD).pin_memory()
+    for _ in range(max(1, args.warmup // 2)):
+        a.copy_(hA, non_blocking=True); b.copy_(hB, non_blocking=True); c.copy_(hC, non_blocking=True)
+        dd = d0  # reuse the device RHS buffer
+        dd.copy_(hD, non_blocking=True)
+        solve(plan, a, b, c, dd, m, nsys, nrow)
+        out_h.copy_(dd, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier(ws)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        a.copy_(hA, non_blocking=True); b.copy_(hB, non_blocking=True); c.copy_(hC, non_blocking=True)
+        d0.copy_(hD, non_blocking=True)
+        solve(plan, a, b, c, d0, m, nsys, nrow)
+        out_h.copy_(d0, non_blocking=True)
+    e1.record(st)
+    torch.cuda.synchronize()
+    barrier(ws)
+    e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws, dev)
+    h2d = 3 * hA.numel() * 8 + hD.numel() * 8
+    d2h = hD.numel() * 8
+
+    # Variants: the two-stage split and the long lines (fewer steps).
+    variants = {}
+    plan.destroy()
+    del a, b, c, d0, dpool, hA, hB, hC, hD, keep, w
+    torch.cuda.empty_cache()
+    for name, vm, vns, vn, vp, vdelta in VARIANTS:
+        vw, _ = make_workload(vm, vns, vn, vdelta, dev)
+        va, vb, vc, vd = (torch.from_numpy(x).to(dev) for x in vw.arrays)
+        vplan = pbt.BtdmaGpuPlan().create(vm, vns, vn, vp)
+        ksteps = max(3, args.steps // 2)
+        vs = time_device(vplan, (va, vb, vc), [vd], vm, vns, vn, ksteps, 3, ws, dev, solve)
+        vs = max_over_ranks(vs, ws, dev)
+        t = pbt.solve_noncyclic_profiled(vplan, va, vb, vc, vd.clone(), vm, vns, vn)
+        vrows = vns * vn
+        variants[name] = {
+            "m": vm, "nsys": vns, "nrow": vn, "nseg": vp,
+            "block_rows_per_s": ws * vrows * ksteps / vs,
+            "ms_per_step": vs / ksteps * 1e3,
+            "algorithmic_gbs": vrows * bytes_per_row(vm) / (vs / ksteps) / 1e9,
+            "phases_ms": {"local": t.local_compute * 1e3, "reduced": t.reduced_compute * 1e3,
+                          "update": t.update_compute * 1e3},
+        }
+        vplan.destroy()
+        del va, vb, vc, vd, vw
+        torch.cuda.empty_cache()
+
+    result = {
+        "metric": "block-rows/s (chosen method at <=1e-10 rel err; plain FP64)",
+        "value": value,
+        "unit": "block-rows/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded Philox4x32-10, diagonally dominant, delta=1.2)",
+        "config": {"workload": f"pencil batch m={m}, nsys={nsys}, N={nrow}, P={nseg}, FP64", "m": m,
+                   "nsys": nsys, "nrow": nrow, "nseg": nseg, "method": "fp64 block Thomas (pivoted LU)",
+                   "l2": "inputs 11.4 GB > L2 (no flush needed)", "parallelism": f"replicas x{ws}"},
+        "backward_err": backward_err,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peaks["source"], "bytes_per_row": bytes_per_row(m)},
+        "fp64": {"achieved_tflops": fp64_rate, "flops_per_row": fp64_flops_per_row_thomas(m)},
+        "e2e": {"value": ws * rows * args.steps / e2e_s, "unit": "block-rows/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "variants": variants,
+    }
+    if rank == 0:
+        result["cpu_baseline"] = cpu_baseline(m, nrow, nseg, DELTA, target_s=args.cpu_seconds)
+        print(json.dumps(result), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference algorithm's CPU path on the host cores, a bounded sample per step."""
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from pascal_btdma_gb300 import synth
+
+    threads = O.default_threads()
+    m, nrow, nseg = M, NROW, NSEG
+    nsys_s = 4096
+    w = synth.dominant(m, nsys_s, nrow, seed=SEED, delta=DELTA)
+    cpu = [O.gpu_to_cpu(m, nsys_s, nrow, k < 3, x) for k, x in enumerate(w.arrays)]
+    times = []
+    for i in range(args.warmup + args.steps):
+        arrs = [x.copy() for x in cpu]
+        t0 = time.perf_counter()
+        O.solve_noncyclic_cpu(m, nsys_s, nrow, nseg, *arrs, nthreads=threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    secs = sum(times)
+    rows = nsys_s * nrow
+    value = rows * args.steps / secs
+    sample = (f"{nsys_s} of the {NSYS} systems per step (m={m}, N={nrow}, P={nseg}); oracle C port of "
+              f"mod_btdma_cpu on {threads} threads")
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "block-rows/s (chosen method at <=1e-10 rel err; plain FP64)",
+        "value": value, "unit": "block-rows/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox4x32-10, delta=1.2)",
+        "config": {"workload": f"pencil batch m={m}, nsys={NSYS}, N={nrow}, P={nseg}, FP64", "m": m,
+                   "nsys": NSYS, "nrow": nrow, "nseg": nseg},
+        "cpu_baseline": {"value": value, "unit": "block-rows/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "block-rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

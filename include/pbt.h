@@ -1,0 +1,179 @@
+/*
+ * pbt.h -- C ABI of the GB300 batched block-tridiagonal solver (libpbt.so).
+ *
+ * Drop-in for PaScaL_BTDMA's plan / solve / destroy path:
+ *
+ *   reference (Fortran, Fortran_Original/src/mod_btdma_gpu_v2.f90)
+ *     btdma_makeplan_gpu_v2(plan, m, nsys, nrow_sub, comm)   :70-109
+ *     btdma_many_mpi_gpu_v2(A, B, C, D, m, nsys, nrow_sub, plan) :131-167
+ *     btdma_many_mpi_gpu_v2_profiled(..., plan, timing)     :169-198
+ *     btdma_many_cycl_mpi_gpu_v2(A, B, C, D, m, nsys, nrow_sub, plan) :200-239
+ *     btdma_cleanplan_gpu_v2(plan)                          :111-129
+ *   reference (C++, CUDA_CXX_Port/include/pascal_btdma_cuda.hpp)
+ *     BtdmaGpuPlan::create(m, nsys, nrow, comm, mode)       :128-132
+ *     solve_noncyclic(plan, a, b, c, d, m, nsys, nrow, stream) :137-145
+ *     solve_noncyclic_profiled(..., timings, stream)        :147-156
+ *     solve_cyclic(plan, a, b, c, d, m, nsys, nrow, stream) :158-166
+ *     BtdmaGpuPlan::destroy()                               :134
+ *
+ * One GPU replaces the reference's MPI communicator: the `comm` argument
+ * becomes `nseg`, the number P of segments each line is split into (one
+ * segment per former MPI rank), and `nrow` is the FULL line length N (all P
+ * segments live in the same arrays).  With nseg = 1 the call is identical to
+ * a one-rank reference call.
+ *
+ * Arrays are device pointers in the reference GPU layout (column-major
+ * Fortran A(nsys, nrow, m, m), D(nsys, nrow, m)):
+ *   A[sys + nsys*(row + nrow*(i + m*j))],  D[sys + nsys*(row + nrow*i)]
+ * with (i, j) the row and column inside the m x m block
+ * (pascal_btdma_cuda.hpp:46-65).  System `sys` solves
+ *   A_q x_{q-1} + B_q x_q + C_q x_{q+1} = d_q,   q = 0 .. nrow-1,
+ * where the non-cyclic solve never reads A_0 or C_{nrow-1} (they act as
+ * zero, as in the reference) and the cyclic solve couples row 0 to row
+ * nrow-1 through them.
+ *
+ * In-place contract (as in the reference, mod_btdma_gpu_v2.f90:618-919):
+ * D is overwritten with the solution x.  B is never written.  A and C are
+ * not written either unless the plan was created with PBT_FLAG_INPLACE, in
+ * which case they receive the elimination factors (the reference's A', C')
+ * and the plan needs no factor workspace.
+ *
+ * Errors: every entry point returns a pbt_status instead of throwing;
+ * pbt_last_error_string() gives the message of the last failure on the
+ * calling thread (the reference throws CudaError / std::invalid_argument /
+ * std::runtime_error / std::logic_error, pascal_btdma_cuda.hpp:20-22 and
+ * pascal_btdma_cuda.cu:862-870, 912-919, 956-967, 1063-1075).
+ *
+ * Threading: a plan owns device workspace; two solves on one plan must not
+ * overlap on the GPU (same rule as the reference plan).  Solves are
+ * asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream)
+ * and never synchronise the host, except the *_profiled entry, which
+ * synchronises to read its event timings.
+ */
+#ifndef PBT_H
+#define PBT_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBT_MAX_BLOCK 10
+
+typedef enum pbt_status {
+    PBT_OK = 0,
+    PBT_EINVAL = 1,       /* bad argument or plan/array mismatch (std::invalid_argument) */
+    PBT_ECUDA = 2,        /* a CUDA runtime call failed (CudaError) */
+    PBT_ESTATE = 3,       /* null or destroyed plan (std::runtime_error) */
+    PBT_EUNSUPPORTED = 4, /* combination not provided (std::logic_error) */
+    PBT_ENOMEM = 5,       /* device workspace allocation failed */
+    PBT_ESINGULAR = 6     /* a zero pivot was met in some block (pbt_plan_status) */
+} pbt_status;
+
+/* Arithmetic of the solve. */
+typedef enum pbt_precision {
+    PBT_PREC_FP64 = 0,        /* plain FP64 arithmetic, partial-pivot LU per block */
+    PBT_PREC_FF = 1,          /* FP64 data, float-float (two-FP32) arithmetic on the FP32 pipes */
+    PBT_PREC_FP32_REFINE = 2  /* FP32 factorisation + FP64-residual iterative refinement */
+} pbt_precision;
+
+/* Plan flags. */
+#define PBT_FLAG_CYCLIC 0x1u           /* periodic lines: plan for pbt_solve_cyclic */
+#define PBT_FLAG_INPLACE 0x2u          /* A, C receive the elimination factors; no factor workspace */
+#define PBT_FLAG_REFERENCE_METHOD 0x4u /* always run the two-stage (modified Thomas) method, even at nseg = 1 */
+
+typedef struct pbt_plan_desc {
+    int m;                 /* block size, 1..PBT_MAX_BLOCK */
+    int nsys;              /* number of independent systems */
+    int nrow;              /* block rows per system (full line length N) */
+    int nseg;              /* segments per line (P); >= 3 rows each when P > 1 */
+    int precision;         /* pbt_precision */
+    unsigned flags;        /* PBT_FLAG_* */
+    double tol;            /* PBT_PREC_FP32_REFINE: target relative correction size */
+    int max_iter;          /* PBT_PREC_FP32_REFINE: refinement iteration cap */
+    int threads_per_block; /* 0 = choose automatically */
+    int reserved[7];
+} pbt_plan_desc;
+
+/* Phase times of one solve in seconds; the same six fields as the
+ * reference's BtdmaSolveTimings (pascal_btdma_cuda.hpp:24-39) and
+ * BTDMA_TIMING_gpu_v2 (mod_btdma_gpu_v2.f90:38-45).  On one GPU the two
+ * exchange phases move no data and read as the time of the (empty)
+ * interval between the compute phases. */
+typedef struct pbt_timings {
+    double total;
+    double local_compute;
+    double forward_exchange;
+    double reduced_compute;
+    double backward_exchange;
+    double update_compute;
+} pbt_timings;
+
+typedef struct pbt_plan pbt_plan;
+
+/* Fill `desc` with defaults: nseg = 1, FP64, no flags, tol = 1e-12,
+ * max_iter = 8. */
+void pbt_plan_desc_init(pbt_plan_desc* desc);
+
+/* Replaces BtdmaGpuPlan::create(m, nsys, nrow, comm) (pascal_btdma_cuda.cu:956-1005)
+ * and btdma_makeplan_gpu_v2 (mod_btdma_gpu_v2.f90:70-109): validates the
+ * sizes and allocates the device workspace on the current device.
+ * Non-cyclic, FP64. */
+int pbt_plan_create(pbt_plan** plan, int m, int nsys, int nrow, int nseg);
+
+/* As pbt_plan_create with every option of pbt_plan_desc. */
+int pbt_plan_create_ex(pbt_plan** plan, const pbt_plan_desc* desc);
+
+/* Replaces BtdmaGpuPlan::destroy (pascal_btdma_cuda.cu:1007-1033) and
+ * btdma_cleanplan_gpu_v2 (mod_btdma_gpu_v2.f90:111-129).  NULL is a no-op. */
+int pbt_plan_destroy(pbt_plan* plan);
+
+/* Replaces solve_noncyclic (pascal_btdma_cuda.cu:1035-1045, impl :853-908)
+ * and btdma_many_mpi_gpu_v2 (mod_btdma_gpu_v2.f90:131-167).  m, nsys, nrow
+ * must equal the plan's (PBT_EINVAL otherwise, like the reference's check at
+ * pascal_btdma_cuda.cu:868-870). */
+int pbt_solve_noncyclic(pbt_plan* plan, double* a, double* b, double* c, double* d,
+                        int m, int nsys, int nrow, void* stream);
+
+/* Replaces solve_noncyclic_profiled (pascal_btdma_cuda.cu:1047-1061) and
+ * btdma_many_mpi_gpu_v2_profiled (mod_btdma_gpu_v2.f90:169-198).  `timings`
+ * may be NULL.  Synchronises `stream`. */
+int pbt_solve_noncyclic_profiled(pbt_plan* plan, double* a, double* b, double* c, double* d,
+                                 int m, int nsys, int nrow, pbt_timings* timings, void* stream);
+
+/* Replaces solve_cyclic (pascal_btdma_cuda.cu:1063-1075, which throws in the
+ * reference port) and btdma_many_cycl_mpi_gpu_v2 (mod_btdma_gpu_v2.f90:200-239).
+ * The plan must carry PBT_FLAG_CYCLIC and nseg >= 2. */
+int pbt_solve_cyclic(pbt_plan* plan, double* a, double* b, double* c, double* d,
+                     int m, int nsys, int nrow, void* stream);
+
+/* Synchronises the plan's last stream and reports through *nsingular how
+ * many zero pivots the solves since the previous call met (the reference has
+ * no such report; its dgesv-less GPU path divides by zero silently).  Returns
+ * PBT_ESINGULAR when *nsingular > 0.  nsingular may be NULL. */
+int pbt_plan_status(pbt_plan* plan, long long* nsingular);
+
+/* Copies the plan's creation parameters into *desc. */
+int pbt_plan_get_desc(const pbt_plan* plan, pbt_plan_desc* desc);
+
+/* Device workspace owned by the plan, in bytes. */
+size_t pbt_plan_workspace_bytes(const pbt_plan* plan);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* pbt_last_error_string(void);
+
+/* Rows [first, last] of part `part` of the inclusive range [start, end]
+ * split into `nparts` parts, the remainder going to the low parts.
+ * Replaces partition_1d (pascal_btdma_cuda.cu:921-930) and mpiutil_para
+ * (Fortran_Original/src/mpiutil.f90:27-48, there 1-based). */
+void pbt_partition_1d(int start, int end, int nparts, int part, int* first, int* last);
+
+/* Library version as an integer, major*10000 + minor*100 + patch. */
+int pbt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBT_H */

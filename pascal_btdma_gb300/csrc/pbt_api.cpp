@@ -1,0 +1,402 @@
+// pbt_api.cpp -- the C ABI of include/pbt.h: plan object, argument checks,
+// workspace, stage dispatch and phase timing.
+//
+// Stage sequence of one solve (reference: btdma_many_mpi_gpu_v2,
+// Fortran_Original/src/mod_btdma_gpu_v2.f90:131-167, and solve_noncyclic_impl,
+// CUDA_CXX_Port/src/pascal_btdma_cuda.cu:853-908):
+//   nseg == 1, non-cyclic, not forced to the reference method:
+//       one launch, plain block Thomas on the whole line.
+//   otherwise:
+//       local (modified elimination of every segment, reduced rows written
+//       into the reduced system) -> reduced solve (non-cyclic or cyclic) ->
+//       update.  The reference's two all-to-all exchanges have no
+//       counterpart: the reduced rows never leave device memory.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "pbt_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(PBT_ECUDA, m);
+}
+
+}  // namespace
+
+struct pbt_plan {
+    pbt_plan_desc desc;
+    int device = 0;
+    bool thomas = false;  // single-segment plain block Thomas path
+    double* aw = nullptr;  // factor workspace (nullptr when in place)
+    double* cw = nullptr;
+    double* ra = nullptr;
+    double* rc = nullptr;
+    double* rd = nullptr;
+    double* re = nullptr;
+    unsigned long long* status = nullptr;
+    size_t bytes = 0;
+    cudaStream_t last_stream = nullptr;
+    unsigned magic = 0x50425450u;  // "PBTP"
+};
+
+namespace {
+
+constexpr unsigned kMagic = 0x50425450u;
+
+int check_plan(const pbt_plan* p) {
+    if (p == nullptr) return fail(PBT_ESTATE, "solve called with a null plan");
+    if (p->magic != kMagic) return fail(PBT_ESTATE, "solve called with a destroyed or corrupt plan");
+    return PBT_OK;
+}
+
+int pick_tpb(const pbt_plan_desc& d, int work_items) {
+    if (d.threads_per_block > 0) return d.threads_per_block;
+    // Enough CTAs to cover every SM when the batch is small: the FP64 pipe is
+    // the bound, so one warp per SM already saturates it.
+    int tpb = 128;
+    while (tpb > 32 && (work_items + tpb - 1) / tpb < 2 * 152) tpb /= 2;
+    return tpb;
+}
+
+#define PBT_DISPATCH(NAME, FN)                                             \
+    cudaError_t NAME(int m, const pbt::SolveArgs& g) {                    \
+        switch (m) {                                                       \
+            case 1: return pbt::FN<1>(g);                                  \
+            case 2: return pbt::FN<2>(g);                                  \
+            case 3: return pbt::FN<3>(g);                                  \
+            case 4: return pbt::FN<4>(g);                                  \
+            case 5: return pbt::FN<5>(g);                                  \
+            case 6: return pbt::FN<6>(g);                                  \
+            case 7: return pbt::FN<7>(g);                                  \
+            case 8: return pbt::FN<8>(g);                                  \
+            case 9: return pbt::FN<9>(g);                                  \
+            case 10: return pbt::FN<10>(g);                                \
+            default: return cudaErrorInvalidValue;                         \
+        }                                                                  \
+    }
+
+PBT_DISPATCH(run_thomas, launch_fp64_thomas)
+PBT_DISPATCH(run_modi, launch_fp64_modi)
+PBT_DISPATCH(run_reduced, launch_fp64_reduced)
+PBT_DISPATCH(run_reduced_cyclic, launch_fp64_reduced_cyclic)
+PBT_DISPATCH(run_update, launch_fp64_update)
+
+int validate(const pbt_plan_desc& d) {
+    char buf[256];
+    if (d.m < 1 || d.m > PBT_MAX_BLOCK) {
+        std::snprintf(buf, sizeof buf, "plan: block size m=%d outside 1..%d", d.m, PBT_MAX_BLOCK);
+        return fail(PBT_EINVAL, buf);
+    }
+    if (d.nsys <= 0 || d.nrow < 2) {
+        std::snprintf(buf, sizeof buf, "plan: requires nsys > 0 and nrow >= 2 (nsys=%d, nrow=%d)", d.nsys, d.nrow);
+        return fail(PBT_EINVAL, buf);
+    }
+    if (d.nseg < 1 || d.nrow < 2 * d.nseg) {
+        std::snprintf(buf, sizeof buf, "plan: nseg=%d must be >= 1 with at least 2 rows per segment (nrow=%d)",
+                      d.nseg, d.nrow);
+        return fail(PBT_EINVAL, buf);
+    }
+    if (d.nseg > 1 && d.nrow < 3 * d.nseg) {
+        // A 2-row segment makes the reference's reduced row 1 couple to the
+        // next segment's first row instead of its own last row, so the
+        // two-stage method returns a wrong x; refuse instead.
+        std::snprintf(buf, sizeof buf,
+                      "plan: with nseg=%d > 1 every segment needs >= 3 rows (nrow=%d < %d)", d.nseg, d.nrow,
+                      3 * d.nseg);
+        return fail(PBT_EINVAL, buf);
+    }
+    if ((d.flags & PBT_FLAG_CYCLIC) && d.nseg < 2) {
+        return fail(PBT_EINVAL, "plan: the cyclic solve needs nseg >= 2 (a reduced system of at least 4 rows)");
+    }
+    if (d.precision != PBT_PREC_FP64) {
+        return fail(PBT_EUNSUPPORTED, "plan: this build provides the FP64 precision only");
+    }
+    if (d.threads_per_block != 0 &&
+        (d.threads_per_block < 32 || d.threads_per_block > 128 || d.threads_per_block % 32 != 0)) {
+        return fail(PBT_EINVAL, "plan: threads_per_block must be 0 or a multiple of 32 in 32..128");
+    }
+    const unsigned known = PBT_FLAG_CYCLIC | PBT_FLAG_INPLACE | PBT_FLAG_REFERENCE_METHOD;
+    if (d.flags & ~known) return fail(PBT_EINVAL, "plan: unknown flag bits");
+    return PBT_OK;
+}
+
+void free_plan(pbt_plan* p) {
+    cudaFree(p->aw);
+    cudaFree(p->cw);
+    cudaFree(p->ra);
+    cudaFree(p->rc);
+    cudaFree(p->rd);
+    cudaFree(p->re);
+    cudaFree(p->status);
+    p->aw = p->cw = p->ra = p->rc = p->rd = p->re = nullptr;
+    p->status = nullptr;
+}
+
+int alloc(pbt_plan* p, double** ptr, size_t n) {
+    if (n == 0) return PBT_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(ptr), n * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "plan: cudaMalloc of %zu bytes failed: %s", n * sizeof(double),
+                      cudaGetErrorString(e));
+        return fail(e == cudaErrorMemoryAllocation ? PBT_ENOMEM : PBT_ECUDA, buf);
+    }
+    p->bytes += n * sizeof(double);
+    return PBT_OK;
+}
+
+pbt::SolveArgs make_args(pbt_plan* p, double* a, double* b, double* c, double* d, cudaStream_t s,
+                         int work_items) {
+    const bool inplace = (p->desc.flags & PBT_FLAG_INPLACE) != 0;
+    pbt::SolveArgs g;
+    g.a = a;
+    g.b = b;
+    g.c = c;
+    g.d = d;
+    g.aw = inplace ? a : p->aw;
+    g.cw = inplace ? c : p->cw;
+    g.ra = p->ra;
+    g.rc = p->rc;
+    g.rd = p->rd;
+    g.re = p->re;
+    g.status = p->status;
+    g.nsys = p->desc.nsys;
+    g.nrow = p->desc.nrow;
+    g.nseg = p->desc.nseg;
+    g.tpb = pick_tpb(p->desc, work_items);
+    g.stream = s;
+    return g;
+}
+
+struct EventSet {
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool ok = false;
+    explicit EventSet(bool make) {
+        if (!make) return;
+        ok = true;
+        for (auto& e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) ok = false;
+    }
+    ~EventSet() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow,
+               bool cyclic, pbt_timings* t, void* stream) {
+    int rc = check_plan(p);
+    if (rc) return rc;
+    const pbt_plan_desc& ds = p->desc;
+    if (m != ds.m || nsys != ds.nsys || nrow != ds.nrow) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "solve dimensions (m=%d, nsys=%d, nrow=%d) do not match the plan (%d, %d, %d)",
+                      m, nsys, nrow, ds.m, ds.nsys, ds.nrow);
+        return fail(PBT_EINVAL, buf);
+    }
+    if (cyclic != ((ds.flags & PBT_FLAG_CYCLIC) != 0)) {
+        return fail(PBT_EINVAL, cyclic ? "cyclic solve on a plan created without PBT_FLAG_CYCLIC"
+                                       : "non-cyclic solve on a plan created with PBT_FLAG_CYCLIC");
+    }
+    if (!a || !b || !c || !d) return fail(PBT_EINVAL, "solve: null array pointer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    p->last_stream = s;
+
+    const bool timed = (t != nullptr);
+    EventSet evs(timed);
+    if (timed && !evs.ok) return fail(PBT_ECUDA, "solve_profiled: cudaEventCreate failed");
+    auto mark = [&](int i) -> cudaError_t { return timed ? cudaEventRecord(evs.ev[i], s) : cudaSuccess; };
+
+    cudaError_t e;
+    if ((e = mark(0)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    if (p->thomas) {
+        e = run_thomas(m, make_args(p, a, b, c, d, s, nsys));
+        if (e != cudaSuccess) return cuda_fail(e, "block Thomas launch");
+        for (int i = 1; i < 5; ++i)
+            if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    } else {
+        pbt::SolveArgs g = make_args(p, a, b, c, d, s, nsys * ds.nseg);
+        e = run_modi(m, g);
+        if (e != cudaSuccess) return cuda_fail(e, "local-stage launch");
+        if ((e = mark(1)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+        if ((e = mark(2)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+        pbt::SolveArgs g2 = make_args(p, a, b, c, d, s, nsys);
+        e = cyclic ? run_reduced_cyclic(m, g2) : run_reduced(m, g2);
+        if (e != cudaSuccess) return cuda_fail(e, "reduced-stage launch");
+        if ((e = mark(3)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+        e = run_update(m, g);
+        if (e != cudaSuccess) return cuda_fail(e, "update-stage launch");
+        if ((e = mark(4)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    }
+    if (timed) {
+        if ((e = cudaEventSynchronize(evs.ev[4])) != cudaSuccess) return cuda_fail(e, "solve_profiled");
+        float ms[4] = {0, 0, 0, 0};
+        for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], evs.ev[i], evs.ev[i + 1]);
+        float tot = 0;
+        cudaEventElapsedTime(&tot, evs.ev[0], evs.ev[4]);
+        if (p->thomas) {
+            // One fused launch: all of it is local compute.
+            t->local_compute = tot * 1e-3;
+            t->forward_exchange = t->reduced_compute = t->backward_exchange = t->update_compute = 0.0;
+        } else {
+            t->local_compute = ms[0] * 1e-3;
+            t->forward_exchange = ms[1] * 1e-3;
+            t->reduced_compute = ms[2] * 1e-3;
+            t->backward_exchange = 0.0;
+            t->update_compute = ms[3] * 1e-3;
+        }
+        t->total = tot * 1e-3;
+    }
+    return PBT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pbt_plan_desc_init(pbt_plan_desc* d) {
+    if (!d) return;
+    std::memset(d, 0, sizeof *d);
+    d->nseg = 1;
+    d->precision = PBT_PREC_FP64;
+    d->tol = 1e-12;
+    d->max_iter = 8;
+}
+
+int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
+    if (!out || !desc) return fail(PBT_EINVAL, "plan_create: null argument");
+    *out = nullptr;
+    int rc = validate(*desc);
+    if (rc) return rc;
+    pbt_plan* p = new (std::nothrow) pbt_plan();
+    if (!p) return fail(PBT_ENOMEM, "plan_create: host allocation failed");
+    p->desc = *desc;
+    cudaGetDevice(&p->device);
+    const auto& d = *desc;
+    const bool inplace = (d.flags & PBT_FLAG_INPLACE) != 0;
+    const bool cyclic = (d.flags & PBT_FLAG_CYCLIC) != 0;
+    p->thomas = (d.nseg == 1) && !cyclic && !(d.flags & PBT_FLAG_REFERENCE_METHOD);
+    const size_t mm = (size_t)d.m * d.m;
+    const size_t rows = (size_t)d.nsys * d.nrow;
+    const size_t rrows = (size_t)d.nsys * 2 * d.nseg;
+    if (!inplace) {
+        if ((rc = alloc(p, &p->cw, mm * rows))) goto fail_out;
+        if (!p->thomas && (rc = alloc(p, &p->aw, mm * rows))) goto fail_out;
+    }
+    if (!p->thomas) {
+        if ((rc = alloc(p, &p->ra, mm * rrows))) goto fail_out;
+        if ((rc = alloc(p, &p->rc, mm * rrows))) goto fail_out;
+        if ((rc = alloc(p, &p->rd, (size_t)d.m * rrows))) goto fail_out;
+        if (cyclic && (rc = alloc(p, &p->re, mm * rrows))) goto fail_out;
+    }
+    {
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->status), sizeof(unsigned long long));
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "plan_create: status word");
+            goto fail_out;
+        }
+        e = cudaMemset(p->status, 0, sizeof(unsigned long long));
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "plan_create: status word");
+            goto fail_out;
+        }
+    }
+    *out = p;
+    return PBT_OK;
+fail_out:
+    free_plan(p);
+    p->magic = 0;
+    delete p;
+    return rc;
+}
+
+int pbt_plan_create(pbt_plan** out, int m, int nsys, int nrow, int nseg) {
+    pbt_plan_desc d;
+    pbt_plan_desc_init(&d);
+    d.m = m;
+    d.nsys = nsys;
+    d.nrow = nrow;
+    d.nseg = nseg;
+    return pbt_plan_create_ex(out, &d);
+}
+
+int pbt_plan_destroy(pbt_plan* p) {
+    if (!p) return PBT_OK;
+    if (p->magic != kMagic) return fail(PBT_ESTATE, "plan_destroy: destroyed or corrupt plan");
+    free_plan(p);
+    p->magic = 0;
+    delete p;
+    return PBT_OK;
+}
+
+int pbt_solve_noncyclic(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow,
+                        void* stream) {
+    return solve_impl(p, a, b, c, d, m, nsys, nrow, false, nullptr, stream);
+}
+
+int pbt_solve_noncyclic_profiled(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys,
+                                 int nrow, pbt_timings* t, void* stream) {
+    pbt_timings local;
+    return solve_impl(p, a, b, c, d, m, nsys, nrow, false, t ? t : &local, stream);
+}
+
+int pbt_solve_cyclic(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow,
+                     void* stream) {
+    return solve_impl(p, a, b, c, d, m, nsys, nrow, true, nullptr, stream);
+}
+
+int pbt_plan_status(pbt_plan* p, long long* nsingular) {
+    int rc = check_plan(p);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(p->last_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "plan_status: stream synchronize");
+    unsigned long long v = 0;
+    e = cudaMemcpy(&v, p->status, sizeof v, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "plan_status: read");
+    e = cudaMemset(p->status, 0, sizeof v);
+    if (e != cudaSuccess) return cuda_fail(e, "plan_status: reset");
+    if (nsingular) *nsingular = (long long)v;
+    if (v) return fail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
+    return PBT_OK;
+}
+
+int pbt_plan_get_desc(const pbt_plan* p, pbt_plan_desc* d) {
+    int rc = check_plan(p);
+    if (rc) return rc;
+    if (!d) return fail(PBT_EINVAL, "plan_get_desc: null desc");
+    *d = p->desc;
+    return PBT_OK;
+}
+
+size_t pbt_plan_workspace_bytes(const pbt_plan* p) {
+    if (!p || p->magic != kMagic) return 0;
+    return p->bytes + sizeof(unsigned long long);
+}
+
+const char* pbt_last_error_string(void) { return g_last_error.c_str(); }
+
+void pbt_partition_1d(int start, int end, int nparts, int part, int* first, int* last) {
+    const int n = end - start + 1;
+    const int base = n / nparts, rem = n % nparts;
+    const int f = part * base + start + (part < rem ? part : rem);
+    if (first) *first = f;
+    if (last) *last = f + base - 1 + (rem > part ? 1 : 0);
+}
+
+int pbt_version(void) { return 100; }
+
+}  // extern "C"

@@ -1,0 +1,44 @@
+// pbt_internal.h -- plan object and kernel-launch interface shared by the
+// C ABI (pbt_api.cpp) and the per-block-size kernel objects (*_inst.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "../../include/pbt.h"
+
+namespace pbt {
+
+// Arguments of one solve as the kernels see them.  All arrays use the
+// reference GPU layout (see include/pbt.h); the reduced-system arrays use the
+// same layout with nrow replaced by 2*nseg:
+//   ra[sys + nsys*(r + 2*nseg*(i + m*j))], rd[sys + nsys*(r + 2*nseg*i)].
+struct SolveArgs {
+    const double* a;  // A (read; also written when aw == a)
+    const double* b;  // B (read only)
+    const double* c;  // C (read; also written when cw == c)
+    double* d;        // D: right-hand side in, solution out
+    double* aw;       // where the factors A' go: == a (in place) or workspace
+    double* cw;       // where the factors C' go: == c (in place) or workspace
+    double* ra;       // reduced rows: A'
+    double* rc;       // reduced rows: C'
+    double* rd;       // reduced rows: d', then the reduced solution
+    double* re;       // cyclic fill-in column of the reduced system
+    unsigned long long* status;  // zero pivots met
+    int nsys;
+    int nrow;
+    int nseg;
+    int tpb;  // threads per block
+    cudaStream_t stream;
+};
+
+// FP64 kernels, one explicit instantiation per block size M (1..PBT_MAX_BLOCK)
+// in pbt_fp64_inst.cu.  Each launcher returns cudaGetLastError().
+template <int M> cudaError_t launch_fp64_thomas(const SolveArgs& g);
+template <int M> cudaError_t launch_fp64_modi(const SolveArgs& g);
+template <int M> cudaError_t launch_fp64_reduced(const SolveArgs& g);
+template <int M> cudaError_t launch_fp64_reduced_cyclic(const SolveArgs& g);
+template <int M> cudaError_t launch_fp64_update(const SolveArgs& g);
+
+}  // namespace pbt

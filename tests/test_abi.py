@@ -1,0 +1,121 @@
+"""The C ABI boundary (include/pbt.h): the library loads, exports every
+declared entry point, and rejects bad arguments before touching the GPU
+(CPU only; no compute calls)."""
+import ctypes as C
+import re
+import threading
+from pathlib import Path
+
+import pytest
+
+import pascal_btdma_gb300 as pbt
+from pascal_btdma_gb300 import _native as N
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared(header: str) -> set[str]:
+    text = (ROOT / "include" / header).read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"\b(pbt_[a-z0-9_]+)\s*\(", text))
+
+
+@pytest.mark.parametrize("header,loader", [("pbt.h", N.lib), ("pbt_synth.h", N.synth_lib)])
+def test_every_declared_symbol_is_exported(header, loader):
+    lib = loader()
+    names = declared(header)
+    assert len(names) >= 5
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared in {header} but not exported"
+
+
+def test_python_signatures_cover_header():
+    assert declared("pbt.h") == set(N.SIGNATURES)
+    assert declared("pbt_synth.h") == set(N.SYNTH_SIGNATURES)
+
+
+def test_version_and_partition():
+    assert N.lib().pbt_version() >= 100
+    for n, p in [(128, 4), (10, 3), (2048, 8), (7, 7)]:
+        firsts = [pbt.partition_1d(0, n - 1, p, r) for r in range(p)]
+        assert firsts[0][0] == 0 and firsts[-1][1] == n - 1
+        for (f0, l0), (f1, l1) in zip(firsts, firsts[1:]):
+            assert f1 == l0 + 1 and (l0 - f0) >= (l1 - f1) >= (l0 - f0) - 1
+
+
+def test_desc_defaults():
+    d = N.PlanDesc()
+    N.lib().pbt_plan_desc_init(C.byref(d))
+    assert (d.nseg, d.precision, d.flags, d.max_iter) == (1, N.PBT_PREC_FP64, 0, 8)
+    assert d.tol == 1e-12
+
+
+def create(**kw):
+    d = N.PlanDesc()
+    N.lib().pbt_plan_desc_init(C.byref(d))
+    base = dict(m=3, nsys=16, nrow=12, nseg=1)
+    base.update(kw)
+    for k, v in base.items():
+        setattr(d, k, v)
+    h = C.c_void_p()
+    rc = N.lib().pbt_plan_create_ex(C.byref(h), C.byref(d))
+    return rc, h, N.last_error()
+
+
+@pytest.mark.parametrize(
+    "kw,code,msg",
+    [
+        (dict(m=0), N.PBT_EINVAL, "block size"),
+        (dict(m=11), N.PBT_EINVAL, "block size"),
+        (dict(nsys=0), N.PBT_EINVAL, "nsys > 0"),
+        (dict(nrow=1), N.PBT_EINVAL, "nrow >= 2"),
+        (dict(nseg=0), N.PBT_EINVAL, "nseg"),
+        (dict(nrow=8, nseg=3), N.PBT_EINVAL, "nseg"),
+        (dict(nrow=10, nseg=4), N.PBT_EINVAL, ">= 3 rows"),
+        (dict(flags=N.PBT_FLAG_CYCLIC), N.PBT_EINVAL, "cyclic"),
+        (dict(flags=0x100), N.PBT_EINVAL, "unknown flag"),
+        (dict(threads_per_block=48), N.PBT_EINVAL, "threads_per_block"),
+        (dict(precision=7), N.PBT_EUNSUPPORTED, "precision"),
+    ],
+)
+def test_plan_create_rejects(kw, code, msg):
+    rc, h, err = create(**kw)
+    assert rc == code and not h.value
+    assert msg in err
+
+
+def test_null_plan_calls():
+    lib = N.lib()
+    assert lib.pbt_plan_destroy(None) == N.PBT_OK
+    z = C.c_void_p(0)
+    rc = lib.pbt_solve_noncyclic(None, z, z, z, z, 3, 16, 12, None)
+    assert rc == N.PBT_ESTATE and "null plan" in N.last_error()
+    assert lib.pbt_plan_status(None, None) == N.PBT_ESTATE
+    assert lib.pbt_plan_workspace_bytes(None) == 0
+
+
+def test_last_error_is_per_thread():
+    create(m=0)
+    seen = []
+    t = threading.Thread(target=lambda: seen.append(N.last_error()))
+    t.start()
+    t.join()
+    assert seen == [""] and "block size" in N.last_error()
+
+
+def test_python_mirror_errors():
+    plan = pbt.BtdmaGpuPlan()
+    with pytest.raises(ValueError, match="block size"):
+        plan.create(11, 16, 12)
+    with pytest.raises(ValueError, match=">= 3 rows"):
+        plan.create(3, 16, 10, nseg=4)
+    with pytest.raises(ValueError, match="unknown precision"):
+        plan.create(3, 16, 12, precision="fp16")
+    with pytest.raises(RuntimeError, match="uncreated"):
+        pbt.solve_noncyclic(plan, 0, 0, 0, 0, 3, 16, 12)
+    assert not plan.created
+
+
+def test_index_helpers_match_reference_layout():
+    assert pbt.matrix_index(1, 2, 0, 1, 4, 5, 3) == 1 + 4 * (2 + 5 * (0 + 3 * 1))
+    assert pbt.vector_index(3, 4, 2, 8, 6) == 3 + 8 * (4 + 6 * 2)

@@ -1,0 +1,174 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the CPU
+oracle on the same seeded inputs.  Plain FP64 must match within 1e-12
+relative per system (max|x - x_oracle| / max|x_oracle|; the oracle pivots
+like LAPACK, the GPU pivots the same way but fuses multiply-adds)."""
+import numpy as np
+import pytest
+import torch
+
+import pascal_btdma_gb300 as pbt
+from pascal_btdma_gb300 import synth
+from conftest import per_system_relerr
+from gpu_util import column_subset, gpu_solve, oracle_solve, subset, to_dev
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+GRID = [  # m, nsys, nrow, nseg
+    (1, 37, 10, 1), (1, 37, 12, 4), (2, 65, 9, 1), (2, 65, 9, 3), (3, 33, 12, 4), (3, 129, 13, 2),
+    (4, 31, 40, 8), (5, 70, 24, 3), (5, 64, 256, 16), (6, 17, 18, 6), (7, 9, 9, 3), (8, 20, 16, 5),
+    (9, 11, 12, 4), (10, 7, 30, 3), (3, 40, 3, 1), (4, 5, 2, 1), (4, 300, 128, 1), (2, 1, 2, 1),
+]
+
+
+@pytest.mark.parametrize("m,nsys,nrow,nseg", GRID)
+@pytest.mark.parametrize("delta", [1.05, 2.0])
+def test_noncyclic_matches_oracle(cuda, m, nsys, nrow, nseg, delta):
+    w = synth.dominant(m, nsys, nrow, seed=1000 * m + nseg, delta=delta)
+    (_, B, _, D), singular = gpu_solve(w, nseg)
+    ref = oracle_solve(w, nseg)
+    assert singular == 0
+    assert per_system_relerr(m, nsys, nrow, D, ref.D) <= TOL
+    assert np.array_equal(B, w.B)
+
+
+def test_small_config(cuda):
+    """m=3, nsys=1024, N=128 split into 4 segments of 32, delta=2.0."""
+    w = synth.dominant(3, 1024, 128, seed=1, delta=2.0)
+    (A, _, C, D), _ = gpu_solve(w, 4)
+    ref = oracle_solve(w, 4)
+    assert per_system_relerr(3, 1024, 128, D, ref.D) <= TOL
+    assert np.array_equal(A, w.A) and np.array_equal(C, w.C)  # not in place by default
+
+
+@pytest.mark.parametrize("nseg", [1, 2, 4])
+def test_inplace_side_effects_match_reference(cuda, nseg):
+    """PBT_FLAG_INPLACE + reference method: A and C receive the same A', C' as the reference."""
+    m, nsys, nrow = 4, 96, 24
+    w = synth.dominant(m, nsys, nrow, seed=77, delta=1.5)
+    (A, _, C, D), _ = gpu_solve(w, nseg, inplace=True, reference_method=True)
+    ref = oracle_solve(w, nseg)
+    assert per_system_relerr(m, nsys, nrow, D, ref.D) <= TOL
+    scale = max(np.abs(ref.A).max(), np.abs(ref.C).max())
+    assert np.abs(A - ref.A).max() <= 1e-11 * scale
+    assert np.abs(C - ref.C).max() <= 1e-11 * scale
+
+
+@pytest.mark.parametrize("m,nsys,nrow,nseg", [(1, 33, 8, 2), (2, 40, 16, 4), (3, 70, 12, 3), (4, 64, 24, 6), (5, 31, 30, 5), (8, 9, 12, 2)])
+def test_cyclic_matches_oracle(cuda, m, nsys, nrow, nseg):
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=5 + m, delta=1.5, flags=0)
+    (_, _, _, D), _ = gpu_solve(w, nseg, cyclic=True)
+    ref = oracle_solve(w, nseg, cyclic=True)
+    assert per_system_relerr(m, nsys, nrow, D, ref.D) <= TOL
+
+
+def test_manufactured_solution(cuda):
+    w = synth.manufactured(3, 256, 64, seed=2)
+    (_, _, _, D), _ = gpu_solve(w, 4)
+    ref = oracle_solve(w, 4)
+    assert per_system_relerr(3, 256, 64, D, ref.D) <= 1e-10
+
+
+def test_reference_signatures_on_gpu(cuda):
+    """The reference's recorded first-solve signatures, full batch sizes."""
+    import json
+    from pathlib import Path
+
+    rows = json.loads((Path(__file__).parent / "golden" / "signatures.json").read_text())["rows"]
+    for row in rows:
+        m, nsys, nrow, nseg = row["m"], row["nsys"], row["n3"], row["nseg"]
+        nm = nsys * nrow * m * m
+        if nm > 6e8:
+            nsys = max(1, int(6e8 // (nrow * m * m)))
+        dev = cuda
+        eye = torch.eye(m, dtype=torch.float64, device=dev)
+        blk = eye.T.reshape(m * m, 1).expand(m * m, nsys * nrow).reshape(-1)  # plane (i + m*j) = delta_ij
+        a = (0.25 * blk).contiguous()
+        b = (2.0 * blk).contiguous()
+        c = (0.25 * blk).contiguous()
+        d = torch.ones(nsys * nrow * m, dtype=torch.float64, device=dev)
+        with pbt.BtdmaGpuPlan() as plan:
+            plan.create(m, nsys, nrow, nseg)
+            pbt.solve_noncyclic(plan, a, b, c, d, m, nsys, nrow)
+        x = d.reshape(m, nrow, nsys)
+        k = row["nsys"] / nsys
+        assert float(d.sum()) * k == pytest.approx(row["solution_sum"], rel=1e-9)
+        assert float(torch.sqrt((d * d).sum())) * np.sqrt(k) == pytest.approx(row["solution_l2"], rel=1e-9)
+        assert float(d.abs().max()) == pytest.approx(row["solution_linf"], rel=1e-14)
+        for z, key in ((0, "sample_z0"), (nrow // 2, "sample_zmid"), (nrow - 1, "sample_zlast")):
+            assert float(x[0, z, 0]) == pytest.approx(row[key], rel=1e-14)
+        del a, b, c, d
+
+
+def test_singular_block_is_reported(cuda):
+    m, nsys, nrow = 3, 64, 10
+    w = synth.dominant(m, nsys, nrow, seed=3, delta=1.5)
+    B = w.B.reshape(m, m, nrow, nsys)
+    B[:, :, 4, 5] = 0.0  # system 5, row 4: B - A C' has a zero row/col -> zero pivot
+    w.A.reshape(m, m, nrow, nsys)[:, :, 4, 5] = 0.0
+    (_, _, _, D), singular = gpu_solve(w, 1)
+    assert singular >= 1
+    x = D.reshape(m, nrow, nsys)
+    assert np.isfinite(np.delete(x, 5, axis=2)).all()  # other systems unaffected
+
+
+def test_profiled_timings(cuda):
+    w = synth.dominant(4, 4096, 64, seed=4, delta=1.5)
+    a, b, c, d = to_dev(w.arrays, cuda)
+    for nseg in (1, 4):
+        with pbt.BtdmaGpuPlan() as plan:
+            plan.create(4, 4096, 64, nseg)
+            t = pbt.solve_noncyclic_profiled(plan, a, b, c, d.clone(), 4, 4096, 64)
+        assert t.total > 0 and t.local_compute > 0
+        assert t.computation() <= t.total * 1.001 + 1e-6
+        if nseg > 1:
+            assert t.reduced_compute > 0 and t.update_compute > 0
+
+
+def test_plan_mismatch_and_reuse(cuda):
+    w = synth.dominant(3, 64, 12, seed=5, delta=2.0)
+    a, b, c, d = to_dev(w.arrays, cuda)
+    plan = pbt.BtdmaGpuPlan().create(3, 64, 12, 2)
+    with pytest.raises(ValueError, match="do not match"):
+        pbt.solve_noncyclic(plan, a, b, c, d, 3, 64, 13)
+    with pytest.raises(ValueError, match="PBT_FLAG_CYCLIC|cyclic"):
+        pbt.solve_cyclic(plan, a, b, c, d, 3, 64, 12)
+    # the same plan solves twice with the same result
+    d1, d2 = d.clone(), d.clone()
+    pbt.solve_noncyclic(plan, a, b, c, d1, 3, 64, 12)
+    pbt.solve_noncyclic(plan, a, b, c, d2, 3, 64, 12)
+    assert torch.equal(d1, d2)
+    plan.destroy()
+    with pytest.raises(RuntimeError, match="uncreated"):
+        pbt.solve_noncyclic(plan, a, b, c, d, 3, 64, 12)
+
+
+def test_side_stream(cuda):
+    w = synth.dominant(5, 512, 32, seed=6, delta=1.2)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        (_, _, _, D), _ = gpu_solve(w, 2, stream=s)
+    ref = oracle_solve(w, 2)
+    assert per_system_relerr(5, 512, 32, D, ref.D) <= TOL
+
+
+FULL = [  # the production-size configurations: m, nsys, nrow, nseg, delta
+    (5, 65536, 256, 1, 1.2),
+    (5, 65536, 256, 16, 1.2),
+    (4, 256, 32768, 128, 1.2),
+]
+
+
+@pytest.mark.parametrize("m,nsys,nrow,nseg,delta", FULL, ids=["pencil_P1", "pencil_P16", "long_lines_P128"])
+def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta):
+    """Full batch on the GPU; 48 of its systems re-solved by the oracle.
+    Systems are independent, so this checks those systems exactly."""
+    w = synth.dominant(m, nsys, nrow, seed=2024, delta=delta)
+    (_, _, _, D), singular = gpu_solve(w, nseg)
+    assert singular == 0
+    rng = np.random.default_rng(0)
+    pick = np.unique(np.concatenate([[0, nsys - 1], rng.choice(nsys, size=min(nsys, 46), replace=False)]))
+    ref = oracle_solve(subset(w, pick), nseg)
+    got = column_subset(m, nsys, nrow, D, pick)
+    assert per_system_relerr(m, len(pick), nrow, got, ref.D) <= TOL
+    assert np.isfinite(D).all()
