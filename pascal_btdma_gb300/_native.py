@@ -80,6 +80,10 @@ SIGNATURES = {
     "pbt_version": (C.c_int, []),
 }
 
+PROBE_SIGNATURES = {
+    "pbt_probe_fma_rates": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+}
+
 SYNTH_SIGNATURES = {
     "pbt_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "pbt_synth_uniform": (C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
@@ -116,7 +120,7 @@ def lib() -> C.CDLL:
     """The loaded libpbt.so (raises if it has not been built)."""
     global _lib
     if _lib is None:
-        _lib = _bind(LIB_PATH, SIGNATURES)
+        _lib = _bind(LIB_PATH, {**SIGNATURES, **PROBE_SIGNATURES})
     return _lib
 
 

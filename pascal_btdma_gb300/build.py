@@ -34,7 +34,7 @@ MAX_BLOCK = 10
 
 # Families of kernels instantiated per block size: (source, object stem).
 PER_M_SOURCES = [("pbt_fp64_inst.cu", "fp64")]
-HOST_SOURCES = ["pbt_api.cpp"]
+HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu"]
 
 
 def _nvcc() -> str:
@@ -45,7 +45,7 @@ def _nvcc() -> str:
 
 
 def _headers() -> list[Path]:
-    return sorted(list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h")))
+    return sorted(list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [INCLUDE / "pbt.h"])
 
 
 def _stale(out: Path, deps: list[Path]) -> bool:
@@ -77,7 +77,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     for src in HOST_SOURCES:
         obj = BUILD / (Path(src).stem + ".o")
         objs.append(obj)
-        if _stale(obj, [CSRC / src] + hdrs):
+        if _stale(obj, [CSRC / src] + hdrs + sorted(INCLUDE.glob("*.h"))):
             tasks.append((obj, [nvcc, *NVCC_FLAGS, "-x", "cu", "-c", str(CSRC / src), "-o", str(obj)]))
     jobs = jobs or max(2, os.cpu_count() or 2)
     if tasks:

@@ -1,0 +1,66 @@
+// pbt_probe.cu -- FP64 / FP32 FMA rate probes (include/pbt_probe.h).
+#include <cuda_runtime.h>
+
+#include "../../include/pbt.h"
+#include "../../include/pbt_probe.h"
+
+namespace {
+
+template <typename T, int CH>
+__global__ void fma_chains(T* out, int iters, T a, T b) {
+    T x[CH];
+#pragma unroll
+    for (int k = 0; k < CH; ++k) x[k] = (T)(threadIdx.x * 1e-7) + (T)k;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int k = 0; k < CH; ++k) x[k] = fma(x[k], a, b);
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < CH; ++k) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename T>
+double rate(int sms, int iters, cudaError_t& err) {
+    const int blocks = sms * 4, threads = 256, ch = 8;
+    T* out = nullptr;
+    err = cudaMalloc(&out, sizeof(T) * blocks * threads);
+    if (err != cudaSuccess) return 0.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fma_chains<T, 8><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(e0);
+        fma_chains<T, 8><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    return (double)blocks * threads * ch * iters / (best * 1e-3);
+}
+
+}  // namespace
+
+extern "C" int pbt_probe_fma_rates(double* fp64, double* fp32) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PBT_ECUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return PBT_ECUDA;
+    cudaError_t e = cudaSuccess;
+    if (fp64) {
+        *fp64 = rate<double>(sms, 2048, e);
+        if (e != cudaSuccess) return PBT_ECUDA;
+    }
+    if (fp32) {
+        *fp32 = rate<float>(sms, 65536, e);
+        if (e != cudaSuccess) return PBT_ECUDA;
+    }
+    return PBT_OK;
+}
