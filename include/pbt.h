@@ -148,6 +148,32 @@ int pbt_solve_noncyclic_profiled(pbt_plan* plan, double* a, double* b, double* c
 int pbt_solve_cyclic(pbt_plan* plan, double* a, double* b, double* c, double* d,
                      int m, int nsys, int nrow, void* stream);
 
+/* Solve without a plan and without allocating device memory.
+ *
+ * No counterpart in the reference.  It exists for callers that cannot call
+ * cudaMalloc: applications that give all device memory to their own pool
+ * allocator at start-up and forbid later allocations, and time-stepping loops
+ * that must not call cudaMalloc / cudaFree (which can synchronise the device)
+ * while other streams are busy.  Every plan-based entry allocates workspace
+ * in pbt_plan_create; this one allocates nothing: it runs the two-stage method
+ * (nseg segments per line; nseg = 1 runs it with one segment) in place --
+ * A <- A', C <- C', D <- x, exactly the reference's side effects -- and keeps
+ * its only scratch, the reduced system, in a fixed array of 4 Mi doubles
+ * (32 MiB) compiled into the library, held on every GPU that loads the library
+ * until the process exits.
+ *
+ * Limit: nsys * 2 * nseg * (2*m*m + m) doubles, each of the three reduced
+ * arrays rounded up to a multiple of 32, must fit in 4 Mi doubles; larger
+ * calls return PBT_EINVAL with the sizes in pbt_last_error_string().  Other
+ * argument rules as pbt_plan_create.  The first call on each device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the array
+ * and it keeps the previous call's contents (each call rewrites what it
+ * reads), so two calls that overlap on the GPU race: serialise them on one
+ * stream.  Zero pivots are not reported by this entry. */
+int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, double* d,
+                                int m, int nsys, int nrow, int nseg, void* stream);
+
 /* Synchronises the plan's last stream and reports through *nsingular how
  * many zero pivots the solves since the previous call met (the reference has
  * no such report; its dgesv-less GPU path divides by zero silently).  Returns

@@ -72,6 +72,7 @@ SIGNATURES = {
         [_P, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.POINTER(Timings), _P],
     ),
     "pbt_solve_cyclic": (C.c_int, [_P, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, _P]),
+    "pbt_solve_noncyclic_noalloc": (C.c_int, [_D, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "pbt_plan_status": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "pbt_plan_get_desc": (C.c_int, [_P, C.POINTER(PlanDesc)]),
     "pbt_plan_workspace_bytes": (C.c_size_t, [_P]),

@@ -34,7 +34,7 @@ MAX_BLOCK = 10
 
 # Families of kernels instantiated per block size: (source, object stem).
 PER_M_SOURCES = [("pbt_fp64_inst.cu", "fp64")]
-HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu"]
+HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu", "pbt_noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -266,6 +266,8 @@ int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
 
 }  // namespace
 
+int pbt::set_last_error(int code, const char* msg) { return fail(code, msg ? msg : ""); }
+
 extern "C" {
 
 void pbt_plan_desc_init(pbt_plan_desc* d) {

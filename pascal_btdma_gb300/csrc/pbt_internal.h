@@ -41,4 +41,8 @@ template <int M> cudaError_t launch_fp64_reduced(const SolveArgs& g);
 template <int M> cudaError_t launch_fp64_reduced_cyclic(const SolveArgs& g);
 template <int M> cudaError_t launch_fp64_update(const SolveArgs& g);
 
+// Records the message returned by pbt_last_error_string() on this thread and
+// returns `code` (defined in pbt_api.cpp).
+int set_last_error(int code, const char* msg);
+
 }  // namespace pbt
