@@ -33,7 +33,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 MAX_BLOCK = 10
 
 # Families of kernels instantiated per block size: (source, object stem).
-PER_M_SOURCES = [("pbt_fp64_inst.cu", "fp64")]
+PER_M_SOURCES = [("pbt_inst.cu", "F64"), ("pbt_inst.cu", "FF")]
 HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu", "pbt_noalloc.cu"]
 
 
@@ -70,10 +70,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     objs: list[Path] = []
     for src, stem in PER_M_SOURCES:
         for m in range(1, MAX_BLOCK + 1):
-            obj = BUILD / f"{stem}_m{m}.o"
+            obj = BUILD / f"{stem.lower()}_m{m}.o"
             objs.append(obj)
             if _stale(obj, [CSRC / src] + hdrs):
-                tasks.append((obj, [nvcc, *NVCC_FLAGS, f"-DPBT_M={m}", "-c", str(CSRC / src), "-o", str(obj)]))
+                tasks.append((obj, [nvcc, *NVCC_FLAGS, f"-DPBT_M={m}", f"-DPBT_NUM=pbt::{stem}", "-c",
+                                    str(CSRC / src), "-o", str(obj)]))
     for src in HOST_SOURCES:
         obj = BUILD / (Path(src).stem + ".o")
         objs.append(obj)

@@ -71,28 +71,34 @@ int pick_tpb(const pbt_plan_desc& d, int work_items) {
     return tpb;
 }
 
-#define PBT_DISPATCH(NAME, FN)                                             \
-    cudaError_t NAME(int m, const pbt::SolveArgs& g) {                    \
-        switch (m) {                                                       \
-            case 1: return pbt::FN<1>(g);                                  \
-            case 2: return pbt::FN<2>(g);                                  \
-            case 3: return pbt::FN<3>(g);                                  \
-            case 4: return pbt::FN<4>(g);                                  \
-            case 5: return pbt::FN<5>(g);                                  \
-            case 6: return pbt::FN<6>(g);                                  \
-            case 7: return pbt::FN<7>(g);                                  \
-            case 8: return pbt::FN<8>(g);                                  \
-            case 9: return pbt::FN<9>(g);                                  \
-            case 10: return pbt::FN<10>(g);                                \
-            default: return cudaErrorInvalidValue;                         \
-        }                                                                  \
+#define PBT_DISPATCH_M(NUM, FN)                                            \
+    switch (m) {                                                           \
+        case 1: return pbt::FN<NUM, 1>(g);                                 \
+        case 2: return pbt::FN<NUM, 2>(g);                                 \
+        case 3: return pbt::FN<NUM, 3>(g);                                 \
+        case 4: return pbt::FN<NUM, 4>(g);                                 \
+        case 5: return pbt::FN<NUM, 5>(g);                                 \
+        case 6: return pbt::FN<NUM, 6>(g);                                 \
+        case 7: return pbt::FN<NUM, 7>(g);                                 \
+        case 8: return pbt::FN<NUM, 8>(g);                                 \
+        case 9: return pbt::FN<NUM, 9>(g);                                 \
+        case 10: return pbt::FN<NUM, 10>(g);                               \
+        default: return cudaErrorInvalidValue;                             \
     }
 
-PBT_DISPATCH(run_thomas, launch_fp64_thomas)
-PBT_DISPATCH(run_modi, launch_fp64_modi)
-PBT_DISPATCH(run_reduced, launch_fp64_reduced)
-PBT_DISPATCH(run_reduced_cyclic, launch_fp64_reduced_cyclic)
-PBT_DISPATCH(run_update, launch_fp64_update)
+#define PBT_DISPATCH(NAME, FN)                                             \
+    cudaError_t NAME(int prec, int m, const pbt::SolveArgs& g) {          \
+        if (prec == PBT_PREC_FF) {                                         \
+            PBT_DISPATCH_M(pbt::FF, FN)                                    \
+        }                                                                  \
+        PBT_DISPATCH_M(pbt::F64, FN)                                       \
+    }
+
+PBT_DISPATCH(run_thomas, launch_thomas)
+PBT_DISPATCH(run_modi, launch_modi)
+PBT_DISPATCH(run_reduced, launch_reduced)
+PBT_DISPATCH(run_reduced_cyclic, launch_reduced_cyclic)
+PBT_DISPATCH(run_update, launch_update)
 
 int validate(const pbt_plan_desc& d) {
     char buf[256];
@@ -121,8 +127,8 @@ int validate(const pbt_plan_desc& d) {
     if ((d.flags & PBT_FLAG_CYCLIC) && d.nseg < 2) {
         return fail(PBT_EINVAL, "plan: the cyclic solve needs nseg >= 2 (a reduced system of at least 4 rows)");
     }
-    if (d.precision != PBT_PREC_FP64) {
-        return fail(PBT_EUNSUPPORTED, "plan: this build provides the FP64 precision only");
+    if (d.precision != PBT_PREC_FP64 && d.precision != PBT_PREC_FF) {
+        return fail(PBT_EUNSUPPORTED, "plan: precision not provided by this build (FP64 and FF are)");
     }
     if (d.threads_per_block != 0 &&
         (d.threads_per_block < 32 || d.threads_per_block > 128 || d.threads_per_block % 32 != 0)) {
@@ -174,6 +180,7 @@ pbt::SolveArgs make_args(pbt_plan* p, double* a, double* b, double* c, double* d
     g.rd = p->rd;
     g.re = p->re;
     g.status = p->status;
+    g.factors_raw = inplace ? 0 : 1;
     g.nsys = p->desc.nsys;
     g.nrow = p->desc.nrow;
     g.nseg = p->desc.nseg;
@@ -224,21 +231,21 @@ int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
     cudaError_t e;
     if ((e = mark(0)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     if (p->thomas) {
-        e = run_thomas(m, make_args(p, a, b, c, d, s, nsys));
+        e = run_thomas(ds.precision, m, make_args(p, a, b, c, d, s, nsys));
         if (e != cudaSuccess) return cuda_fail(e, "block Thomas launch");
         for (int i = 1; i < 5; ++i)
             if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     } else {
         pbt::SolveArgs g = make_args(p, a, b, c, d, s, nsys * ds.nseg);
-        e = run_modi(m, g);
+        e = run_modi(ds.precision, m, g);
         if (e != cudaSuccess) return cuda_fail(e, "local-stage launch");
         if ((e = mark(1)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
         if ((e = mark(2)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
         pbt::SolveArgs g2 = make_args(p, a, b, c, d, s, nsys);
-        e = cyclic ? run_reduced_cyclic(m, g2) : run_reduced(m, g2);
+        e = cyclic ? run_reduced_cyclic(ds.precision, m, g2) : run_reduced(ds.precision, m, g2);
         if (e != cudaSuccess) return cuda_fail(e, "reduced-stage launch");
         if ((e = mark(3)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
-        e = run_update(m, g);
+        e = run_update(ds.precision, m, g);
         if (e != cudaSuccess) return cuda_fail(e, "update-stage launch");
         if ((e = mark(4)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     }

@@ -1,0 +1,21 @@
+// pbt_inst.cu -- explicit instantiation of the solver kernels for one
+// arithmetic and one block size.  The build compiles this file once per
+// (PBT_NUM, PBT_M), PBT_NUM in {F64, FF} and PBT_M in 1..PBT_MAX_BLOCK, so the
+// unrolled variants compile in parallel.
+#if !defined(PBT_M) || !defined(PBT_NUM)
+#error "compile with -DPBT_M=<block size> -DPBT_NUM=<F64|FF>"
+#endif
+
+#if PBT_M > 6
+#define PBT_UNROLL _Pragma("unroll 1")
+#endif
+
+#include "pbt_kernels.cuh"
+
+namespace pbt {
+template cudaError_t launch_thomas<PBT_NUM, PBT_M>(const SolveArgs&);
+template cudaError_t launch_modi<PBT_NUM, PBT_M>(const SolveArgs&);
+template cudaError_t launch_reduced<PBT_NUM, PBT_M>(const SolveArgs&);
+template cudaError_t launch_reduced_cyclic<PBT_NUM, PBT_M>(const SolveArgs&);
+template cudaError_t launch_update<PBT_NUM, PBT_M>(const SolveArgs&);
+}  // namespace pbt

@@ -26,6 +26,7 @@ struct SolveArgs {
     double* rd;       // reduced rows: d', then the reduced solution
     double* re;       // cyclic fill-in column of the reduced system
     unsigned long long* status;  // zero pivots met
+    int factors_raw;  // 1: aw/cw are workspace (raw arithmetic values); 0: caller's A/C (FP64)
     int nsys;
     int nrow;
     int nseg;
@@ -33,13 +34,17 @@ struct SolveArgs {
     cudaStream_t stream;
 };
 
-// FP64 kernels, one explicit instantiation per block size M (1..PBT_MAX_BLOCK)
-// in pbt_fp64_inst.cu.  Each launcher returns cudaGetLastError().
-template <int M> cudaError_t launch_fp64_thomas(const SolveArgs& g);
-template <int M> cudaError_t launch_fp64_modi(const SolveArgs& g);
-template <int M> cudaError_t launch_fp64_reduced(const SolveArgs& g);
-template <int M> cudaError_t launch_fp64_reduced_cyclic(const SolveArgs& g);
-template <int M> cudaError_t launch_fp64_update(const SolveArgs& g);
+// The two arithmetics of pbt_num.cuh.
+struct F64;
+struct FF;
+
+// Kernel launchers, explicitly instantiated per arithmetic and block size M
+// (1..PBT_MAX_BLOCK) in pbt_inst.cu.  Each returns cudaGetLastError().
+template <class Num, int M> cudaError_t launch_thomas(const SolveArgs& g);
+template <class Num, int M> cudaError_t launch_modi(const SolveArgs& g);
+template <class Num, int M> cudaError_t launch_reduced(const SolveArgs& g);
+template <class Num, int M> cudaError_t launch_reduced_cyclic(const SolveArgs& g);
+template <class Num, int M> cudaError_t launch_update(const SolveArgs& g);
 
 // Records the message returned by pbt_last_error_string() on this thread and
 // returns `code` (defined in pbt_api.cpp).

@@ -1,0 +1,841 @@
+// pbt_kernels.cuh -- the solver kernels, written once over an arithmetic
+// `Num` (pbt_num.cuh: F64 = plain FP64, FF = float-float on the FP32 pipes)
+// and a compile-time block size M.
+//
+// One thread owns one (system, segment) pair; consecutive threads own
+// consecutive systems, so every block-element access of a warp is one
+// contiguous 256-byte segment of the reference GPU layout
+// X[sys + nsys*(row + nrow*(i + M*j))].  All m x m arithmetic is unrolled.
+//
+//   k_thomas        single-segment fast path: plain block Thomas on the whole
+//                   line (the reduced-solve recurrence of btdma_many_gpu_v2,
+//                   Fortran_Original/src/mod_btdma_gpu_v2.f90:241-350, applied
+//                   to the original rows).  Same x as the two-stage method
+//                   with one segment, at ~40% of its flops.
+//   k_modi          stage 1 of the two-stage method, one segment:
+//                   btdma_many_modi_gpu_v2 (mod_btdma_gpu_v2.f90:618-866).  The
+//                   two reduced rows go straight into the reduced system's
+//                   layout, which replaces the pack + MPI_ALLTOALLV + unpack
+//                   of :1309-1342.
+//   k_reduced       stage 2: block Thomas on the 2P-row reduced system (B = I),
+//                   btdma_many_gpu_v2 (:241-350).
+//   k_reduced_cyclic stage 2 of the cyclic solve: btdma_many_cycl
+//                   (Fortran_Original/src/mod_btdma_cpu.f90:80-183).
+//   k_update        stage 3: x_q = d'_q - A'_q x_first - C'_q x_last
+//                   (btdma_many_update_gpu_v2, mod_btdma_gpu_v2.f90:868-919),
+//                   reading the reduced solution in place (replaces the
+//                   backward MPI_ALLTOALLV of :1344-1374).
+//
+// Storage rules: inputs are FP64 and converted on load (Num::in); the
+// solution is converted on store (Num::out).  Intermediates -- the factors in
+// the plan's workspace, d'/y parked in D, the reduced system -- are raw 8-byte
+// Num values (Num::lds / Num::sts); factors written in place into the
+// caller's A and C are converted to FP64 so those arrays stay valid doubles.
+#pragma once
+
+#include "pbt_block64.cuh"
+#include "pbt_internal.h"
+#include "pbt_num.cuh"
+
+namespace pbt {
+
+// Loop unrolling policy (PBT_UNROLL precedes every m x m loop): fully
+// unrolled by default, so the blocks live in registers.  A translation unit
+// instantiating only M = 7..10 defines PBT_UNROLL as "unroll 1" first: those
+// blocks do not fit in registers anyway, and full unrolling would only
+// multiply compile time (minutes per variant), so their loops stay rolled and
+// the blocks live in local memory.
+#ifndef PBT_UNROLL
+#define PBT_UNROLL _Pragma("unroll")
+#endif
+
+__device__ __forceinline__ void seg_rows(int n, int p, int s, int& first, int& last) {
+    const int base = n / p, rem = n % p;
+    first = s * base + (s < rem ? s : rem);
+    last = first + base + (s < rem ? 1 : 0) - 1;
+}
+
+// ---------------------------------------------------------------------------
+// Gaussian elimination with partial pivoting on [a | b] (M x M, M x NR);
+// the solution a^{-1} b is left in b.  Pivot = first row of maximal |a(i,k)|
+// (LAPACK idamax rule; for FF the high part decides); multipliers are
+// a(i,k) * (1/a(k,k)) as in dgetf2.  Entries are accumulators, normalised
+// only when their row becomes the pivot row.  A zero pivot sets `bad`; the
+// arithmetic goes on (Inf/NaN), like the reference.
+// ---------------------------------------------------------------------------
+template <class Num, int M, int NR>
+__device__ __forceinline__ void gesv(typename Num::Acc (&a)[M][M], typename Num::Acc (&b)[M][NR], bool& bad) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    T rinv[M];
+PBT_UNROLL
+    for (int k = 0; k < M; ++k) {
+        if (k + 1 < M) {
+            int p = k;
+            auto best = Num::key(Num::fin(a[k][k]));
+PBT_UNROLL
+            for (int i = k + 1; i < M; ++i) {
+                const auto v = Num::key(Num::fin(a[i][k]));
+                const bool gt = v > best;
+                best = gt ? v : best;
+                p = gt ? i : p;
+            }
+PBT_UNROLL
+            for (int i = k + 1; i < M; ++i) {
+                const unsigned s = (p == i);
+PBT_UNROLL
+                for (int c = k; c < M; ++c) {
+                    const Acc t = a[k][c];
+                    a[k][c] = Num::asel(s, a[i][c], t);
+                    a[i][c] = Num::asel(s, t, a[i][c]);
+                }
+PBT_UNROLL
+                for (int c = 0; c < NR; ++c) {
+                    const Acc t = b[k][c];
+                    b[k][c] = Num::asel(s, b[i][c], t);
+                    b[i][c] = Num::asel(s, t, b[i][c]);
+                }
+            }
+        }
+        const T piv = Num::fin(a[k][k]);
+        bad |= Num::is_zero(piv);
+        const T r = Num::rcp(piv);
+        rinv[k] = r;
+        T uk[M], bk[NR];
+PBT_UNROLL
+        for (int c = k + 1; c < M; ++c) {
+            uk[c] = Num::fin(a[k][c]);
+            a[k][c] = Num::acc(uk[c]);
+        }
+PBT_UNROLL
+        for (int c = 0; c < NR; ++c) {
+            bk[c] = Num::fin(b[k][c]);
+            b[k][c] = Num::acc(bk[c]);
+        }
+PBT_UNROLL
+        for (int i = k + 1; i < M; ++i) {
+            const T l = Num::mul(Num::fin(a[i][k]), r);
+PBT_UNROLL
+            for (int c = k + 1; c < M; ++c) Num::msub(a[i][c], l, uk[c]);
+PBT_UNROLL
+            for (int c = 0; c < NR; ++c) Num::msub(b[i][c], l, bk[c]);
+        }
+    }
+PBT_UNROLL
+    for (int k = M - 1; k >= 0; --k) {
+PBT_UNROLL
+        for (int c = 0; c < NR; ++c) {
+            const T x = Num::mul(Num::fin(b[k][c]), rinv[k]);
+            b[k][c] = Num::acc(x);
+PBT_UNROLL
+            for (int i = 0; i < k; ++i) Num::msub(b[i][c], Num::fin(a[i][k]), x);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Loads and stores of one block / vector at `base` (= X + sys + nsys*row).
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__device__ __forceinline__ void in_blk(typename Num::T (&x)[M][M], const double* base, size_t plane) {
+PBT_UNROLL
+    for (int j = 0; j < M; ++j)
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) x[i][j] = Num::in(base + (size_t)(i + M * j) * plane);
+}
+template <class Num, int M>
+__device__ __forceinline__ void in_blk_ro(typename Num::T (&x)[M][M], const double* base, size_t plane) {
+PBT_UNROLL
+    for (int j = 0; j < M; ++j)
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) x[i][j] = Num::in_ro(base + (size_t)(i + M * j) * plane);
+}
+template <class Num, int M>
+__device__ __forceinline__ void ld_raw_blk(typename Num::T (&x)[M][M], const double* base, size_t plane) {
+PBT_UNROLL
+    for (int j = 0; j < M; ++j)
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) x[i][j] = Num::lds(base + (size_t)(i + M * j) * plane);
+}
+template <class Num, int M>
+__device__ __forceinline__ void st_raw_blk(double* base, size_t plane, const typename Num::T (&x)[M][M]) {
+PBT_UNROLL
+    for (int j = 0; j < M; ++j)
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) Num::sts(base + (size_t)(i + M * j) * plane, x[i][j]);
+}
+template <class Num, int M>
+__device__ __forceinline__ void ld_raw_vec(typename Num::T (&x)[M], const double* base, size_t plane) {
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) x[i] = Num::lds(base + (size_t)i * plane);
+}
+template <class Num, int M>
+__device__ __forceinline__ void st_raw_vec(double* base, size_t plane, const typename Num::T (&x)[M]) {
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) Num::sts(base + (size_t)i * plane, x[i]);
+}
+template <class Num, int M>
+__device__ __forceinline__ void out_vec(double* base, size_t plane, const typename Num::T (&x)[M]) {
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) Num::out(base + (size_t)i * plane, x[i]);
+}
+// Factor storage: raw in the plan's workspace, FP64 when written in place.
+template <class Num, int M>
+__device__ __forceinline__ void st_fac_blk(double* base, size_t plane, const typename Num::T (&x)[M][M], bool raw) {
+    if (raw || !Num::kIsFF) {
+        st_raw_blk<Num, M>(base, plane, x);
+    } else {
+PBT_UNROLL
+        for (int j = 0; j < M; ++j)
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) Num::out(base + (size_t)(i + M * j) * plane, x[i][j]);
+    }
+}
+template <class Num, int M>
+__device__ __forceinline__ void ld_fac_blk(typename Num::T (&x)[M][M], const double* base, size_t plane, bool raw) {
+    if (raw || !Num::kIsFF)
+        ld_raw_blk<Num, M>(x, base, plane);
+    else
+        in_blk<Num, M>(x, base, plane);
+}
+
+template <class Num, int M>
+__device__ __forceinline__ void to_acc(typename Num::Acc (&d)[M][M], const typename Num::T (&s)[M][M]) {
+PBT_UNROLL
+    for (int i = 0; i < M; ++i)
+PBT_UNROLL
+        for (int j = 0; j < M; ++j) d[i][j] = Num::acc(s[i][j]);
+}
+
+// ---------------------------------------------------------------------------
+// Single-segment block Thomas.  Forward: R_q = B_q - A_q C'_{q-1},
+// [C'_q | y_q] = R_q^{-1} [C_q | d_q - A_q y_{q-1}]; C' goes to cw, y to D.
+// Backward: x_q = y_q - C'_q x_{q+1}.
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_thomas(const SolveArgs g) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int N = g.nrow;
+    const size_t plane0 = (size_t)g.nsys * N;
+    const size_t rs = (size_t)g.nsys;
+    const double* A = g.a + sys;
+    const double* B = g.b + sys;
+    const double* C = g.c + sys;
+    double* D = g.d + sys;
+    double* CW = g.cw + sys;
+    const bool raw = g.factors_raw != 0;
+    bool bad = false;
+
+    T cp[M][M], y[M];
+    for (int q = 0; q < N; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        const bool last = (q == N - 1);
+        Acc r[M][M], x[M][M + 1];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            T ar[M];
+            if (q > 0) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) ar[k] = Num::in(A + o + (size_t)(i + M * k) * plane);
+            }
+            Acc t = Num::acc(Num::in(D + o + (size_t)i * plane));
+            if (q > 0) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(t, ar[k], y[k]);
+            }
+            x[i][M] = t;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc s = Num::acc(Num::in_ro(B + o + (size_t)(i + M * j) * plane));
+                if (q > 0) {
+PBT_UNROLL
+                    for (int k = 0; k < M; ++k) Num::msub(s, ar[k], cp[k][j]);
+                }
+                r[i][j] = s;
+            }
+            mem_fence_compiler();
+        }
+        if (!last) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) x[i][j] = Num::acc(Num::in(C + o + (size_t)(i + M * j) * plane));
+            gesv<Num, M, M + 1>(r, x, bad);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) cp[i][j] = Num::fin(x[i][j]);
+                y[i] = Num::fin(x[i][M]);
+            }
+            st_fac_blk<Num, M>(CW + o, plane, cp, raw);
+            st_raw_vec<Num, M>(D + o, plane, y);
+        } else {
+            Acc xv[M][1];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) xv[i][0] = x[i][M];
+            gesv<Num, M, 1>(r, xv, bad);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) y[i] = Num::fin(xv[i][0]);
+            out_vec<Num, M>(D + o, plane, y);
+        }
+    }
+    for (int q = N - 2; q >= 0; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T c[M][M], t[M];
+        ld_fac_blk<Num, M>(c, CW + o, plane, raw);
+        ld_raw_vec<Num, M>(t, D + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+            t[i] = Num::fin(s);
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) y[i] = t[i];
+        out_vec<Num, M>(D + o, plane, y);
+    }
+    if (bad) atomicAdd(g.status, 1ull);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1: modified elimination of one segment (rows f..l, n = l - f + 1).
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_modi(const SolveArgs g) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int seg = blockIdx.y;
+    int f, l;
+    seg_rows(g.nrow, g.nseg, seg, f, l);
+    const int n = l - f + 1;
+    const size_t plane0 = (size_t)g.nsys * g.nrow;
+    const size_t rs = (size_t)g.nsys;
+    const size_t fo = (size_t)f * rs + sys;
+    const double* A = g.a + fo;
+    const double* B = g.b + fo;
+    const double* C = g.c + fo;
+    double* D = g.d + fo;
+    double* AW = g.aw + fo;
+    double* CW = g.cw + fo;
+    const bool raw = g.factors_raw != 0;
+    const int R = 2 * g.nseg;
+    const size_t rplane = (size_t)g.nsys * R;
+    bool bad = false;
+
+    T ap[M][M], cp[M][M], dp[M];
+    // Rows 1 and 2 of the segment: [A'|C'|d'] = B^{-1}[A|C|d]; rows 3..n:
+    // R = B - A C'_{q-1}; [A'|C'|d'] = R^{-1}[-A A'_{q-1} | C | d - A d'_{q-1}].
+    for (int q = 0; q < n; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        const bool first2 = (q < 2);
+        Acc r[M][M], x[M][2 * M + 1];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            T ar[M];
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) ar[k] = Num::in(A + o + (size_t)(i + M * k) * plane);
+            Acc t = Num::acc(Num::in(D + o + (size_t)i * plane));
+            if (!first2) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(t, ar[k], dp[k]);
+            }
+            x[i][2 * M] = t;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc u = Num::acc(Num::in_ro(B + o + (size_t)(i + M * j) * plane));
+                if (first2) {
+                    x[i][j] = Num::acc(ar[j]);
+                } else {
+                    Acc s = Num::acc0();
+PBT_UNROLL
+                    for (int k = 0; k < M; ++k) {
+                        Num::msub(s, ar[k], ap[k][j]);
+                        Num::msub(u, ar[k], cp[k][j]);
+                    }
+                    x[i][j] = s;
+                }
+                r[i][j] = u;
+            }
+            mem_fence_compiler();
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i)
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) x[i][M + j] = Num::acc(Num::in(C + o + (size_t)(i + M * j) * plane));
+        gesv<Num, M, 2 * M + 1>(r, x, bad);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                ap[i][j] = Num::fin(x[i][j]);
+                cp[i][j] = Num::fin(x[i][M + j]);
+            }
+            dp[i] = Num::fin(x[i][2 * M]);
+        }
+        st_fac_blk<Num, M>(AW + o, plane0, ap, raw);
+        st_fac_blk<Num, M>(CW + o, plane0, cp, raw);
+        st_raw_vec<Num, M>(D + o, plane0, dp);
+    }
+    // Reduced row 2*seg+1 = the segment's last row (A'_n, C'_n, d'_n).
+    {
+        const size_t ro = (size_t)sys + rs * (size_t)(2 * seg + 1);
+        st_raw_blk<Num, M>(g.ra + ro, rplane, ap);
+        st_raw_blk<Num, M>(g.rc + ro, rplane, cp);
+        st_raw_vec<Num, M>(g.rd + ro, rplane, dp);
+    }
+    // Backward sweep, rows n-2 .. 2 (1-based): carried row = q+1.
+    {
+        const int q1 = (n >= 4) ? n - 2 : 1;
+        const size_t o1 = (size_t)q1 * rs;
+        ld_fac_blk<Num, M>(ap, AW + o1, plane0, raw);
+        ld_fac_blk<Num, M>(cp, CW + o1, plane0, raw);
+        ld_raw_vec<Num, M>(dp, D + o1, plane0);
+    }
+    for (int q = n - 3; q >= 1; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T a[M][M], c[M][M], dq[M];
+        ld_fac_blk<Num, M>(a, AW + o, plane, raw);
+        ld_fac_blk<Num, M>(c, CW + o, plane, raw);
+        ld_raw_vec<Num, M>(dq, D + o, plane);
+        // Row by row: row i of the new A', C' needs only row i of C'_q.
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc t = Num::acc(dq[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(t, c[i][k], dp[k]);
+            dq[i] = Num::fin(t);
+            T nc[M];
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc s = Num::acc(a[i][j]);
+                Acc u = Num::acc0();
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) {
+                    Num::msub(s, c[i][k], ap[k][j]);
+                    Num::msub(u, c[i][k], cp[k][j]);
+                }
+                a[i][j] = Num::fin(s);
+                nc[j] = Num::fin(u);
+            }
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) c[i][j] = nc[j];
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                ap[i][j] = a[i][j];
+                cp[i][j] = c[i][j];
+            }
+            dp[i] = dq[i];
+        }
+        st_fac_blk<Num, M>(AW + o, plane, ap, raw);
+        st_fac_blk<Num, M>(CW + o, plane, cp, raw);
+        st_raw_vec<Num, M>(D + o, plane, dp);
+    }
+    // Row 1: R = I - C'_1 A'_2; [A'_1|C'_1|d'_1] = R^{-1}[A'_1 | -C'_1 C'_2 | d'_1 - C'_1 d'_2].
+    {
+        const size_t plane = opaque(plane0);
+        Acc r[M][M], x[M][2 * M + 1];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            T c0[M];
+            if (raw || !Num::kIsFF) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) c0[k] = Num::lds(CW + (size_t)(i + M * k) * plane);
+            } else {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) c0[k] = Num::in(CW + (size_t)(i + M * k) * plane);
+            }
+            Acc t = Num::acc(Num::lds(D + (size_t)i * plane));
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(t, c0[k], dp[k]);
+            x[i][2 * M] = t;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc s = Num::acc(i == j ? Num::one() : Num::zero());
+                Acc u = Num::acc0();
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) {
+                    Num::msub(s, c0[k], ap[k][j]);
+                    Num::msub(u, c0[k], cp[k][j]);
+                }
+                r[i][j] = s;
+                x[i][M + j] = u;
+            }
+            mem_fence_compiler();
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i)
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                const double* p = AW + (size_t)(i + M * j) * plane;
+                x[i][j] = Num::acc((raw || !Num::kIsFF) ? Num::lds(p) : Num::in(p));
+            }
+        gesv<Num, M, 2 * M + 1>(r, x, bad);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                ap[i][j] = Num::fin(x[i][j]);
+                cp[i][j] = Num::fin(x[i][M + j]);
+            }
+            dp[i] = Num::fin(x[i][2 * M]);
+        }
+        st_fac_blk<Num, M>(AW, plane, ap, raw);
+        st_fac_blk<Num, M>(CW, plane, cp, raw);
+        st_raw_vec<Num, M>(D, plane, dp);
+        const size_t ro = (size_t)sys + rs * (size_t)(2 * seg);
+        st_raw_blk<Num, M>(g.ra + ro, rplane, ap);
+        st_raw_blk<Num, M>(g.rc + ro, rplane, cp);
+        st_raw_vec<Num, M>(g.rd + ro, rplane, dp);
+    }
+    if (bad) atomicAdd(g.status, 1ull);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2: block Thomas on the R = 2P reduced rows (B = I).  Row 0's A and
+// row R-1's C are never read.  C' overwrites rc, the solution overwrites rd.
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_reduced(const SolveArgs g) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int R = 2 * g.nseg;
+    const size_t plane0 = (size_t)g.nsys * R;
+    const size_t rs = (size_t)g.nsys;
+    const double* RA = g.ra + sys;
+    double* RC = g.rc + sys;
+    double* RD = g.rd + sys;
+    bool bad = false;
+
+    T cp[M][M], y[M];
+    // Row 0: B = I, so [C'|y] = [C|d] exactly.
+    ld_raw_blk<Num, M>(cp, RC, plane0);
+    ld_raw_vec<Num, M>(y, RD, plane0);
+    for (int q = 1; q < R; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        const bool last = (q == R - 1);
+        Acc r[M][M], x[M][M + 1];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            T ar[M];
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) ar[k] = Num::lds(RA + o + (size_t)(i + M * k) * plane);
+            Acc t = Num::acc(Num::lds(RD + o + (size_t)i * plane));
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(t, ar[k], y[k]);
+            x[i][M] = t;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc s = Num::acc(i == j ? Num::one() : Num::zero());
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(s, ar[k], cp[k][j]);
+                r[i][j] = s;
+            }
+            mem_fence_compiler();
+        }
+        if (!last) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) x[i][j] = Num::acc(Num::lds(RC + o + (size_t)(i + M * j) * plane));
+            gesv<Num, M, M + 1>(r, x, bad);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) cp[i][j] = Num::fin(x[i][j]);
+                y[i] = Num::fin(x[i][M]);
+            }
+            st_raw_blk<Num, M>(RC + o, plane, cp);
+        } else {
+            Acc xv[M][1];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) xv[i][0] = x[i][M];
+            gesv<Num, M, 1>(r, xv, bad);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) y[i] = Num::fin(xv[i][0]);
+        }
+        st_raw_vec<Num, M>(RD + o, plane, y);
+    }
+    for (int q = R - 2; q >= 0; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T c[M][M], t[M];
+        ld_raw_blk<Num, M>(c, RC + o, plane);
+        ld_raw_vec<Num, M>(t, RD + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+            t[i] = Num::fin(s);
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) y[i] = t[i];
+        st_raw_vec<Num, M>(RD + o, plane, y);
+    }
+    if (bad) atomicAdd(g.status, 1ull);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2, cyclic: periodic block Thomas on the R = 2P reduced rows (B = I)
+// with the fill-in column E, following btdma_many_cycl
+// (Fortran_Original/src/mod_btdma_cpu.f90:80-183).  Needs R >= 4.
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_reduced_cyclic(const SolveArgs g) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int R = 2 * g.nseg;
+    const size_t plane0 = (size_t)g.nsys * R;
+    const size_t rs = (size_t)g.nsys;
+    const double* RA = g.ra + sys;
+    double* RC = g.rc + sys;
+    double* RD = g.rd + sys;
+    double* RE = g.re + sys;
+    bool bad = false;
+
+    // Row 1: B = I, so [d'|e'|c'] = [d | -A_1 | C_1] exactly.
+    T cp[M][M], ep[M][M], dp[M];
+    {
+        T a1[M][M];
+        ld_raw_blk<Num, M>(a1, RA + rs, plane0);
+        ld_raw_blk<Num, M>(cp, RC + rs, plane0);
+        ld_raw_vec<Num, M>(dp, RD + rs, plane0);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i)
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) ep[i][j] = Num::neg(a1[i][j]);
+        st_raw_blk<Num, M>(RE + rs, plane0, ep);
+    }
+    // Rows 2..R-1: R_q = I - A_q C'_{q-1};
+    // [d'|e'|c'] = R_q^{-1} [d - A_q d'_{q-1} | e_q - A_q e'_{q-1} | C_q],
+    // with e_q = 0 except e_{R-1} = -C_{R-1}.
+    for (int q = 2; q < R; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        const bool last = (q == R - 1);
+        Acc r[M][M], x[M][2 * M + 1];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            T ar[M];
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) ar[k] = Num::lds(RA + o + (size_t)(i + M * k) * plane);
+            Acc t = Num::acc(Num::lds(RD + o + (size_t)i * plane));
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(t, ar[k], dp[k]);
+            x[i][0] = t;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                const T cij = Num::lds(RC + o + (size_t)(i + M * j) * plane);
+                Acc s = Num::acc(i == j ? Num::one() : Num::zero());
+                Acc u = Num::acc(last ? Num::neg(cij) : Num::zero());
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) {
+                    Num::msub(s, ar[k], cp[k][j]);
+                    Num::msub(u, ar[k], ep[k][j]);
+                }
+                r[i][j] = s;
+                x[i][1 + j] = u;
+                x[i][1 + M + j] = Num::acc(cij);
+            }
+            mem_fence_compiler();
+        }
+        gesv<Num, M, 2 * M + 1>(r, x, bad);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            dp[i] = Num::fin(x[i][0]);
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                ep[i][j] = Num::fin(x[i][1 + j]);
+                cp[i][j] = Num::fin(x[i][1 + M + j]);
+            }
+        }
+        st_raw_vec<Num, M>(RD + o, plane, dp);
+        st_raw_blk<Num, M>(RE + o, plane, ep);
+        st_raw_blk<Num, M>(RC + o, plane, cp);
+    }
+    T elast[M][M], dlast[M];
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) {
+        dlast[i] = dp[i];
+PBT_UNROLL
+        for (int j = 0; j < M; ++j) elast[i][j] = ep[i][j];
+    }
+    // Backward, rows R-2..1: d'_q -= C'_q d'_{q+1}; e'_q -= C'_q e'_{q+1}.
+    for (int q = R - 2; q >= 1; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T c[M][M], e[M][M], t[M];
+        ld_raw_blk<Num, M>(c, RC + o, plane);
+        ld_raw_blk<Num, M>(e, RE + o, plane);
+        ld_raw_vec<Num, M>(t, RD + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], dp[k]);
+            t[i] = Num::fin(s);
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc u = Num::acc(e[i][j]);
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(u, c[i][k], ep[k][j]);
+                e[i][j] = Num::fin(u);
+            }
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            dp[i] = t[i];
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) ep[i][j] = e[i][j];
+        }
+        st_raw_vec<Num, M>(RD + o, plane, dp);
+        st_raw_blk<Num, M>(RE + o, plane, ep);
+    }
+    // Row 0: (I + A_0 e'_{R-1} + C_0 e'_1) x_0 = d_0 - A_0 d'_{R-1} - C_0 d'_1.
+    T x0[M];
+    {
+        T a0[M][M], c0[M][M];
+        ld_raw_blk<Num, M>(a0, RA, plane0);
+        ld_raw_blk<Num, M>(c0, RC, plane0);
+        Acc r[M][M], x[M][1];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc t = Num::acc(Num::lds(RD + (size_t)i * plane0));
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(t, a0[i][k], dlast[k]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(t, c0[i][k], dp[k]);
+            x[i][0] = t;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc s = Num::acc(i == j ? Num::one() : Num::zero());
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::mac(s, a0[i][k], elast[k][j]);
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::mac(s, c0[i][k], ep[k][j]);
+                r[i][j] = s;
+            }
+        }
+        gesv<Num, M, 1>(r, x, bad);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) x0[i] = Num::fin(x[i][0]);
+        st_raw_vec<Num, M>(RD, plane0, x0);
+    }
+    // Rows 1..R-1: x_q = d'_q + e'_q x_0.
+    for (int q = 1; q < R; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T e[M][M], t[M];
+        ld_raw_blk<Num, M>(e, RE + o, plane);
+        ld_raw_vec<Num, M>(t, RD + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::mac(s, e[i][k], x0[k]);
+            t[i] = Num::fin(s);
+        }
+        st_raw_vec<Num, M>(RD + o, plane, t);
+    }
+    if (bad) atomicAdd(g.status, 1ull);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 3: interior update of one segment from the reduced solution.
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_update(const SolveArgs g) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int seg = blockIdx.y;
+    int f, l;
+    seg_rows(g.nrow, g.nseg, seg, f, l);
+    const int n = l - f + 1;
+    const size_t plane0 = (size_t)g.nsys * g.nrow;
+    const size_t rs = (size_t)g.nsys;
+    const size_t fo = (size_t)f * rs + sys;
+    const double* AW = g.aw + fo;
+    const double* CW = g.cw + fo;
+    double* D = g.d + fo;
+    const bool raw = g.factors_raw != 0;
+    const int R = 2 * g.nseg;
+    const size_t rplane = (size_t)g.nsys * R;
+    T x0[M], xn[M];
+    ld_raw_vec<Num, M>(x0, g.rd + sys + rs * (size_t)(2 * seg), rplane);
+    ld_raw_vec<Num, M>(xn, g.rd + sys + rs * (size_t)(2 * seg + 1), rplane);
+    out_vec<Num, M>(D, plane0, x0);
+    out_vec<Num, M>(D + (size_t)(n - 1) * rs, plane0, xn);
+    for (int q = 1; q < n - 1; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T a[M][M], c[M][M], t[M];
+        ld_fac_blk<Num, M>(a, AW + o, plane, raw);
+        ld_fac_blk<Num, M>(c, CW + o, plane, raw);
+        ld_raw_vec<Num, M>(t, D + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, a[i][k], x0[k]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], xn[k]);
+            t[i] = Num::fin(s);
+        }
+        out_vec<Num, M>(D + o, plane, t);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers.
+// ---------------------------------------------------------------------------
+inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) / tpb); }
+
+template <class Num, int M>
+cudaError_t launch_thomas(const SolveArgs& g) {
+    k_thomas<Num, M><<<grid_x(g.nsys, g.tpb), g.tpb, 0, g.stream>>>(g);
+    return cudaGetLastError();
+}
+template <class Num, int M>
+cudaError_t launch_modi(const SolveArgs& g) {
+    dim3 grid(grid_x(g.nsys, g.tpb), (unsigned)g.nseg);
+    k_modi<Num, M><<<grid, g.tpb, 0, g.stream>>>(g);
+    return cudaGetLastError();
+}
+template <class Num, int M>
+cudaError_t launch_reduced(const SolveArgs& g) {
+    k_reduced<Num, M><<<grid_x(g.nsys, g.tpb), g.tpb, 0, g.stream>>>(g);
+    return cudaGetLastError();
+}
+template <class Num, int M>
+cudaError_t launch_reduced_cyclic(const SolveArgs& g) {
+    k_reduced_cyclic<Num, M><<<grid_x(g.nsys, g.tpb), g.tpb, 0, g.stream>>>(g);
+    return cudaGetLastError();
+}
+template <class Num, int M>
+cudaError_t launch_update(const SolveArgs& g) {
+    dim3 grid(grid_x(g.nsys, g.tpb), (unsigned)g.nseg);
+    k_update<Num, M><<<grid, g.tpb, 0, g.stream>>>(g);
+    return cudaGetLastError();
+}
+
+}  // namespace pbt

@@ -69,16 +69,16 @@ int scratch_on_current_device(double** out) {
 
 #define PBT_NOALLOC_DISPATCH(FN)                            \
     switch (m) {                                            \
-        case 1: e = pbt::FN<1>(g); break;                   \
-        case 2: e = pbt::FN<2>(g); break;                   \
-        case 3: e = pbt::FN<3>(g); break;                   \
-        case 4: e = pbt::FN<4>(g); break;                   \
-        case 5: e = pbt::FN<5>(g); break;                   \
-        case 6: e = pbt::FN<6>(g); break;                   \
-        case 7: e = pbt::FN<7>(g); break;                   \
-        case 8: e = pbt::FN<8>(g); break;                   \
-        case 9: e = pbt::FN<9>(g); break;                   \
-        default: e = pbt::FN<10>(g); break;                 \
+        case 1: e = pbt::FN<pbt::F64, 1>(g); break;                   \
+        case 2: e = pbt::FN<pbt::F64, 2>(g); break;                   \
+        case 3: e = pbt::FN<pbt::F64, 3>(g); break;                   \
+        case 4: e = pbt::FN<pbt::F64, 4>(g); break;                   \
+        case 5: e = pbt::FN<pbt::F64, 5>(g); break;                   \
+        case 6: e = pbt::FN<pbt::F64, 6>(g); break;                   \
+        case 7: e = pbt::FN<pbt::F64, 7>(g); break;                   \
+        case 8: e = pbt::FN<pbt::F64, 8>(g); break;                   \
+        case 9: e = pbt::FN<pbt::F64, 9>(g); break;                   \
+        default: e = pbt::FN<pbt::F64, 10>(g); break;                 \
     }
 
 }  // namespace
@@ -124,6 +124,7 @@ extern "C" int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, doub
     g.rd = base + 2 * mat;
     g.re = nullptr;
     g.status = reinterpret_cast<unsigned long long*>(base + kScratchDoubles);
+    g.factors_raw = 0;
     g.nsys = nsys;
     g.nrow = nrow;
     g.nseg = nseg;
@@ -133,7 +134,7 @@ extern "C" int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, doub
     g.stream = static_cast<cudaStream_t>(stream);
 
     cudaError_t e = cudaMemsetAsync(g.status, 0, sizeof(unsigned long long), g.stream);
-    if (e == cudaSuccess) PBT_NOALLOC_DISPATCH(launch_fp64_modi)
+    if (e == cudaSuccess) PBT_NOALLOC_DISPATCH(launch_modi)
     if (e == cudaSuccess) {
         pbt::SolveArgs g2 = g;
         int t2 = 128;
@@ -141,10 +142,10 @@ extern "C" int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, doub
         g2.tpb = t2;
         {
             const pbt::SolveArgs& g = g2;
-            PBT_NOALLOC_DISPATCH(launch_fp64_reduced)
+            PBT_NOALLOC_DISPATCH(launch_reduced)
         }
     }
-    if (e == cudaSuccess) PBT_NOALLOC_DISPATCH(launch_fp64_update)
+    if (e == cudaSuccess) PBT_NOALLOC_DISPATCH(launch_update)
     if (e != cudaSuccess) {
         std::snprintf(buf, sizeof buf, "solve_noncyclic_noalloc: launch failed: %s", cudaGetErrorString(e));
         return pbt::set_last_error(PBT_ECUDA, buf);

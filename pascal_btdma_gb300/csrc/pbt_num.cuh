@@ -1,0 +1,180 @@
+// pbt_num.cuh -- the two arithmetics the solver kernels are written over.
+//
+//   F64: plain IEEE double on the FP64 pipe (1/63 of the FP32 rate on GB300).
+//   FF:  float-float ("double-single") arithmetic on the FP32 pipes.  A value
+//        is an unevaluated sum h + l of two floats with |l| <= ulp(h)/2, which
+//        carries ~47 significant bits.  The operations are built from the
+//        error-free transformations TwoSum (Knuth, TAOCP vol. 2, 4.2.2),
+//        FastTwoSum (Dekker 1971) and the FMA form of TwoProduct (Ogita, Rump,
+//        Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).
+//        Each multiply-accumulate costs 12 FP32 instructions, i.e. ~5x the
+//        FP64 pipe's rate.
+//
+// Every kernel uses the same small interface:
+//   T            register value;  Acc: an accumulator for sums of products
+//   in(p)        load an FP64 input element and convert to T
+//   out(p, v)    convert T to FP64 and store
+//   lds/sts      raw 8-byte workspace slots (no conversion)
+//   acc(x), mac(acc, x, y) (acc += x*y), msub(acc, x, y) (acc -= x*y), fin(acc)
+//   mul, rcp, neg, zero, one, key (|x| as an ordered integer), sel, is_zero
+//
+// FP64 <-> FF conversion uses integer bit operations only, so the FF path
+// issues no FP64 instruction except one DADD per FP64 value it writes.
+#pragma once
+
+#include <cstdint>
+
+namespace pbt {
+
+__device__ __forceinline__ float fsel(unsigned s, float x, float y) {
+    float r;
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %3, 0;\n\tselp.f32 %0, %1, %2, p;\n\t}"
+        : "=f"(r)
+        : "f"(x), "f"(y), "r"(s));
+    return r;
+}
+
+__device__ __forceinline__ double dsel(unsigned s, double x, double y) {
+    double r;
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %3, 0;\n\tselp.f64 %0, %1, %2, p;\n\t}"
+        : "=d"(r)
+        : "d"(x), "d"(y), "r"(s));
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+struct F64 {
+    using T = double;
+    struct Acc {
+        double v;
+    };
+    static constexpr bool kIsFF = false;
+
+    __device__ static __forceinline__ T in(const double* p) { return *p; }
+    __device__ static __forceinline__ T in_ro(const double* p) { return __ldg(p); }
+    __device__ static __forceinline__ void out(double* p, T v) { *p = v; }
+    __device__ static __forceinline__ T lds(const double* p) { return *p; }
+    __device__ static __forceinline__ void sts(double* p, T v) { *p = v; }
+
+    __device__ static __forceinline__ Acc acc(T x) { return {x}; }
+    __device__ static __forceinline__ Acc acc0() { return {0.0}; }
+    __device__ static __forceinline__ void mac(Acc& a, T x, T y) { a.v = fma(x, y, a.v); }
+    __device__ static __forceinline__ void msub(Acc& a, T x, T y) { a.v = fma(-x, y, a.v); }
+    __device__ static __forceinline__ T fin(Acc a) { return a.v; }
+
+    __device__ static __forceinline__ T mul(T a, T b) { return a * b; }
+    __device__ static __forceinline__ T rcp(T a) { return __drcp_rn(a); }
+    __device__ static __forceinline__ T neg(T a) { return -a; }
+    __device__ static __forceinline__ T zero() { return 0.0; }
+    __device__ static __forceinline__ T one() { return 1.0; }
+    __device__ static __forceinline__ unsigned long long key(T a) {
+        return static_cast<unsigned long long>(__double_as_longlong(a)) & 0x7fffffffffffffffull;
+    }
+    __device__ static __forceinline__ T sel(unsigned s, T x, T y) { return dsel(s, x, y); }
+    __device__ static __forceinline__ Acc asel(unsigned s, Acc x, Acc y) { return {dsel(s, x.v, y.v)}; }
+    __device__ static __forceinline__ bool is_zero(T a) { return key(a) == 0ull; }
+};
+
+// ---------------------------------------------------------------------------
+struct ff {
+    float h, l;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // needs |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+struct FF {
+    using T = ff;
+    struct Acc {
+        float s, t;  // unnormalised: value = s + t, t collects rounding errors and low parts
+    };
+    static constexpr bool kIsFF = true;
+
+    // FP64 -> (h, l) by bit manipulation: h = x truncated to 24 significant
+    // bits, l = the next 23 bits.  |x - (h + l)| < 2^-46 |x| for
+    // 2^-100 <= |x| < 2^128; |x| < 2^-126 gives 0, 2^-126 <= |x| < 2^-100
+    // keeps only h (2^-23 relative).
+    __device__ static __forceinline__ T split(double x) {
+        const unsigned hi = static_cast<unsigned>(__double2hiint(x));
+        const unsigned lo = static_cast<unsigned>(__double2loint(x));
+        const unsigned e = (hi >> 20) & 0x7ffu;
+        const unsigned sign = hi & 0x80000000u;
+        // h: rebias the exponent (1023 -> 127) and keep 23 mantissa bits.
+        const unsigned hb = __funnelshift_l(lo, (hi & 0x7fffffffu) - (896u << 20), 3) | sign;
+        // l: the 23 bits below h's mantissa as a float with an explicit leading
+        // one, minus that one (exact).
+        const unsigned eb = (e - 919u) << 23;
+        const float lf = __fsub_rn(__uint_as_float(eb | ((lo >> 6) & 0x7fffffu)), __uint_as_float(eb));
+        const unsigned lb = __float_as_uint(lf) | sign;
+        return {__uint_as_float(e > 896u ? hb : 0u), __uint_as_float(e >= 920u ? lb : 0u)};
+    }
+
+    // float -> double by bit manipulation (normal floats; zero and subnormals -> signed zero).
+    __device__ static __forceinline__ double widen(float f) {
+        const unsigned u = __float_as_uint(f);
+        const unsigned a = u & 0x7fffffffu;
+        const unsigned hiw = (a >= 0x00800000u) ? ((u & 0x80000000u) | ((a >> 3) + (896u << 20))) : (u & 0x80000000u);
+        const unsigned low = (a >= 0x00800000u) ? (a << 29) : 0u;
+        return __hiloint2double(static_cast<int>(hiw), static_cast<int>(low));
+    }
+    __device__ static __forceinline__ double join(T v) { return widen(v.h) + widen(v.l); }
+
+    __device__ static __forceinline__ T in(const double* p) { return split(*p); }
+    __device__ static __forceinline__ T in_ro(const double* p) { return split(__ldg(p)); }
+    __device__ static __forceinline__ void out(double* p, T v) { *p = join(v); }
+    __device__ static __forceinline__ T lds(const double* p) {
+        const float2 f = *reinterpret_cast<const float2*>(p);
+        return {f.x, f.y};
+    }
+    __device__ static __forceinline__ void sts(double* p, T v) { *reinterpret_cast<float2*>(p) = make_float2(v.h, v.l); }
+
+    __device__ static __forceinline__ Acc acc(T x) { return {x.h, x.l}; }
+    __device__ static __forceinline__ Acc acc0() { return {0.f, 0.f}; }
+    // a += x*y: exact product of the high parts, the two cross terms folded
+    // into its error, the high sum by TwoSum, all errors into a.t.
+    __device__ static __forceinline__ void mac(Acc& a, T x, T y) {
+        const float p = __fmul_rn(x.h, y.h);
+        float e = __fmaf_rn(x.h, y.h, -p);
+        e = __fmaf_rn(x.h, y.l, e);
+        e = __fmaf_rn(x.l, y.h, e);
+        const ff s = two_sum(a.s, p);
+        a.s = s.h;
+        a.t = __fadd_rn(a.t, __fadd_rn(s.l, e));
+    }
+    __device__ static __forceinline__ void msub(Acc& a, T x, T y) { mac(a, {-x.h, -x.l}, y); }
+    __device__ static __forceinline__ T fin(Acc a) { return two_sum(a.s, a.t); }
+
+    __device__ static __forceinline__ T mul(T a, T b) {
+        const float p = __fmul_rn(a.h, b.h);
+        float e = __fmaf_rn(a.h, b.h, -p);
+        e = __fmaf_rn(a.h, b.l, e);
+        e = __fmaf_rn(a.l, b.h, e);
+        return fast_two_sum(p, e);
+    }
+    // 1/a: r0 = rcp(a.h); one Newton step r0 + r0*(1 - a*r0), where
+    // 1 - a.h*r0 is exact in one FMA.
+    __device__ static __forceinline__ T rcp(T a) {
+        const float r0 = __frcp_rn(a.h);
+        float e = __fmaf_rn(-a.h, r0, 1.0f);
+        e = __fmaf_rn(-a.l, r0, e);
+        return fast_two_sum(r0, __fmul_rn(r0, e));
+    }
+    __device__ static __forceinline__ T neg(T a) { return {-a.h, -a.l}; }
+    __device__ static __forceinline__ T zero() { return {0.f, 0.f}; }
+    __device__ static __forceinline__ T one() { return {1.f, 0.f}; }
+    __device__ static __forceinline__ unsigned key(T a) { return __float_as_uint(a.h) & 0x7fffffffu; }
+    __device__ static __forceinline__ T sel(unsigned s, T x, T y) { return {fsel(s, x.h, y.h), fsel(s, x.l, y.l)}; }
+    __device__ static __forceinline__ Acc asel(unsigned s, Acc x, Acc y) { return {fsel(s, x.s, y.s), fsel(s, x.t, y.t)}; }
+    __device__ static __forceinline__ bool is_zero(T a) { return key(a) == 0u; }
+};
+
+}  // namespace pbt
