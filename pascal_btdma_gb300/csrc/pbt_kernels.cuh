@@ -72,14 +72,18 @@ PBT_UNROLL
     for (int k = 0; k < M; ++k) {
         if (k + 1 < M) {
             int p = k;
-            auto best = Num::key(Num::fin(a[k][k]));
+            auto best = Num::akey(a[k][k]);
 PBT_UNROLL
             for (int i = k + 1; i < M; ++i) {
-                const auto v = Num::key(Num::fin(a[i][k]));
+                const auto v = Num::akey(a[i][k]);
                 const bool gt = v > best;
                 best = gt ? v : best;
                 p = gt ? i : p;
             }
+            // The swaps cost ~10x the rest of a pivot step in instructions;
+            // skip them when no thread of the warp needs one (the common case
+            // for the diagonally dominant blocks of implicit PDE schemes).
+            if (__any_sync(__activemask(), p != k))
 PBT_UNROLL
             for (int i = k + 1; i < M; ++i) {
                 const unsigned s = (p == i);
@@ -199,6 +203,50 @@ __device__ __forceinline__ void ld_fac_blk(typename Num::T (&x)[M][M], const dou
         in_blk<Num, M>(x, base, plane);
 }
 
+// L2 prefetch of one block row of A, B, C and D for the warp's 32 systems:
+// the 3*M*M + M element planes of the row, each a run of up to 32 doubles
+// that spans at most three 128-byte lines, spread over the lanes (about
+// (3*M*M + M) * 3 / 32 prefetch instructions per lane).  Addresses are
+// clamped to the last system, so a partial warp never names memory outside
+// the arrays.
+template <int M>
+__device__ __forceinline__ void prefetch_row(const double* A, const double* B, const double* C, const double* D,
+                                             int warp_sys0, int nsys, size_t row_off, size_t plane) {
+    constexpr int kPlanes = 3 * M * M + M;
+    const int lane = threadIdx.x & 31;
+#pragma unroll 1
+    for (int idx = lane; idx < 3 * kPlanes; idx += 32) {
+        const int pl = idx / 3, part = idx - 3 * pl;
+        int s = warp_sys0 + (part == 0 ? 0 : (part == 1 ? 16 : 31));
+        s = s < nsys ? s : nsys - 1;
+        const double* base;
+        int e;
+        if (pl < M * M) { base = A; e = pl; }
+        else if (pl < 2 * M * M) { base = B; e = pl - M * M; }
+        else if (pl < 3 * M * M) { base = C; e = pl - 2 * M * M; }
+        else { base = D; e = pl - 3 * M * M; }
+        const double* addr = base + (size_t)s + row_off + (size_t)e * plane;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
+    }
+}
+
+// L2 prefetch of the workspace row (C' and y) read by the backward sweep.
+template <int M>
+__device__ __forceinline__ void prefetch_back_row(const double* CW, const double* D, int warp_sys0, int nsys,
+                                                  size_t row_off, size_t plane) {
+    constexpr int kPlanes = M * M + M;
+    const int lane = threadIdx.x & 31;
+#pragma unroll 1
+    for (int idx = lane; idx < 3 * kPlanes; idx += 32) {
+        const int pl = idx / 3, part = idx - 3 * pl;
+        int s = warp_sys0 + (part == 0 ? 0 : (part == 1 ? 16 : 31));
+        s = s < nsys ? s : nsys - 1;
+        const double* addr = (pl < M * M ? CW + (size_t)pl * plane : D + (size_t)(pl - M * M) * plane) +
+                             (size_t)s + row_off;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
+    }
+}
+
 template <class Num, int M>
 __device__ __forceinline__ void to_acc(typename Num::Acc (&d)[M][M], const typename Num::T (&s)[M][M]) {
 PBT_UNROLL
@@ -212,12 +260,38 @@ PBT_UNROLL
 // [C'_q | y_q] = R_q^{-1} [C_q | d_q - A_q y_{q-1}]; C' goes to cw, y to D.
 // Backward: x_q = y_q - C'_q x_{q+1}.
 // ---------------------------------------------------------------------------
+// Launch shape of k_thomas: 64-thread CTAs, at most 128 registers per
+// thread, i.e. 16 warps per SM, so the 2048 warps of a 65536-system batch run
+// in one wave.  The kernel is bound by memory latency at m = 5 (one thread
+// carries a whole block row), so resident warps matter more than the few
+// spills the cap causes: on GB300 the float-float m = 5 solve runs in 8.3 ms
+// at 128 registers, 9.8 ms at 168 (a second, latency-bound wave) and 9.7 ms at
+// 96 (spills).
+#ifndef PBT_THOMAS_THREADS
+#define PBT_THOMAS_THREADS 64
+#endif
+#ifndef PBT_THOMAS_MAXNREG
+#define PBT_THOMAS_MAXNREG 128
+#endif
+// Rows of A, B, C, D prefetched into L2 ahead of the row being eliminated
+// (measured no gain on GB300: off).
+#ifndef PBT_PREFETCH_ROWS
+#define PBT_PREFETCH_ROWS 0
+#endif
+// Compiler fence between the block rows of one row's loads (keeps only one
+// row of A and B live; 0 lets the compiler hoist all of a row's loads).
+#ifndef PBT_ROW_FENCE
+#define PBT_ROW_FENCE 1
+#endif
+constexpr int kThomasThreads = PBT_THOMAS_THREADS;
+
 template <class Num, int M>
-__global__ void __launch_bounds__(128) k_thomas(const SolveArgs g) {
+__global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
     if (sys >= g.nsys) return;
+    const int warp_sys0 = sys & ~31;
     const int N = g.nrow;
     const size_t plane0 = (size_t)g.nsys * N;
     const size_t rs = (size_t)g.nsys;
@@ -230,10 +304,14 @@ __global__ void __launch_bounds__(128) k_thomas(const SolveArgs g) {
     bool bad = false;
 
     T cp[M][M], y[M];
+    for (int q = 0; q < PBT_PREFETCH_ROWS && q < N; ++q)
+        prefetch_row<M>(g.a, g.b, g.c, g.d, warp_sys0, g.nsys, (size_t)q * rs, plane0);
     for (int q = 0; q < N; ++q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         const bool last = (q == N - 1);
+        if (PBT_PREFETCH_ROWS > 0 && q + PBT_PREFETCH_ROWS < N)
+            prefetch_row<M>(g.a, g.b, g.c, g.d, warp_sys0, g.nsys, o + PBT_PREFETCH_ROWS * rs, plane);
         Acc r[M][M], x[M][M + 1];
 PBT_UNROLL
         for (int i = 0; i < M; ++i) {
@@ -257,7 +335,7 @@ PBT_UNROLL
                 }
                 r[i][j] = s;
             }
-            mem_fence_compiler();
+            if (PBT_ROW_FENCE) mem_fence_compiler();
         }
         if (!last) {
 PBT_UNROLL
@@ -286,6 +364,7 @@ PBT_UNROLL
     for (int q = N - 2; q >= 0; --q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
+        if (q > 0) prefetch_back_row<M>(g.cw, g.d, warp_sys0, g.nsys, o - rs, plane);
         T c[M][M], t[M];
         ld_fac_blk<Num, M>(c, CW + o, plane, raw);
         ld_raw_vec<Num, M>(t, D + o, plane);
@@ -812,7 +891,8 @@ inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) /
 
 template <class Num, int M>
 cudaError_t launch_thomas(const SolveArgs& g) {
-    k_thomas<Num, M><<<grid_x(g.nsys, g.tpb), g.tpb, 0, g.stream>>>(g);
+    const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
+    k_thomas<Num, M><<<grid_x(g.nsys, tpb), tpb, 0, g.stream>>>(g);
     return cudaGetLastError();
 }
 template <class Num, int M>

@@ -72,6 +72,7 @@ struct F64 {
     }
     __device__ static __forceinline__ T sel(unsigned s, T x, T y) { return dsel(s, x, y); }
     __device__ static __forceinline__ Acc asel(unsigned s, Acc x, Acc y) { return {dsel(s, x.v, y.v)}; }
+    __device__ static __forceinline__ unsigned long long akey(Acc a) { return key(a.v); }
     __device__ static __forceinline__ bool is_zero(T a) { return key(a) == 0ull; }
 };
 
@@ -174,6 +175,8 @@ struct FF {
     __device__ static __forceinline__ unsigned key(T a) { return __float_as_uint(a.h) & 0x7fffffffu; }
     __device__ static __forceinline__ T sel(unsigned s, T x, T y) { return {fsel(s, x.h, y.h), fsel(s, x.l, y.l)}; }
     __device__ static __forceinline__ Acc asel(unsigned s, Acc x, Acc y) { return {fsel(s, x.s, y.s), fsel(s, x.t, y.t)}; }
+    // Pivot key of an accumulator: its high part decides.
+    __device__ static __forceinline__ unsigned akey(Acc a) { return __float_as_uint(a.s) & 0x7fffffffu; }
     __device__ static __forceinline__ bool is_zero(T a) { return key(a) == 0u; }
 };
 

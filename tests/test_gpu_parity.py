@@ -13,7 +13,7 @@ from gpu_util import column_subset, gpu_solve, oracle_solve, subset, to_dev
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12      # plain FP64 against the oracle
-TOL_FF = 1e-11   # float-float (~47-bit arithmetic) against the oracle
+TOL_FF = 1e-12   # float-float (~47-bit arithmetic) against the oracle
 PREC_TOL = [("fp64", TOL), ("ff", TOL_FF)]
 
 GRID = [  # m, nsys, nrow, nseg
