@@ -51,6 +51,10 @@ VARIANTS = [  # name, m, nsys, nrow, nseg, delta
     ("pencil_P16", 5, 65536, 256, 16, 1.2),
     ("long_lines_P128", 4, 256, 32768, 128, 1.2),
 ]
+# Mixed precision: the pencil batch with every block row scaled by a
+# log-uniform factor in [1e-3, 1e3]; FP32 factorisation + FP64 residual
+# refinement, and float-float, each against the plain FP64 solution.
+MIXED = [(1.05, 1), (1.05, 16), (1.5, 1), (1.5, 16)]  # (delta, nseg)
 
 
 def bytes_per_row(m: int, width: int = 8) -> int:
@@ -204,7 +208,7 @@ def residual_error(a, b, c, d, x, m, nsys, nrow) -> float:
     return float((num / den).max())
 
 
-def make_workload(m, nsys, nrow, delta, dev, pinned=False):
+def make_workload(m, nsys, nrow, delta, dev, pinned=False, row_scale=False):
     import torch
 
     from pascal_btdma_gb300 import synth
@@ -216,7 +220,7 @@ def make_workload(m, nsys, nrow, delta, dev, pinned=False):
             t = torch.empty(n, dtype=torch.float64, pin_memory=True)
             keep.append(t)
             return t.numpy()
-    w = synth.dominant(m, nsys, nrow, seed=SEED, delta=delta, alloc=alloc)
+    w = synth.dominant(m, nsys, nrow, seed=SEED, delta=delta, alloc=alloc, row_scale=row_scale)
     return w, keep
 
 
@@ -360,6 +364,39 @@ def run_ours(args):
         del va, vb, vc, vd, vw, xs
         torch.cuda.empty_cache()
 
+    mixed = {}
+    by_delta = {}
+    for delta, nseg_m in MIXED:
+        by_delta.setdefault(delta, []).append(nseg_m)
+    for delta, segs in by_delta.items():
+        mw, _ = make_workload(M, NSYS, NROW, delta, dev, row_scale=True)
+        ma, mb, mc, md = (torch.from_numpy(x).to(dev) for x in mw.arrays)
+        mrows = NSYS * NROW
+        for nseg_m in segs:
+            entry = {"delta": delta, "nseg": nseg_m, "row_scale": "log-uniform [1e-3, 1e3]"}
+            ref = md.clone()
+            with pbt.BtdmaGpuPlan() as p64:
+                p64.create(M, NSYS, NROW, nseg_m, precision="fp64")
+                solve(p64, ma, mb, mc, ref, M, NSYS, NROW)
+            for prec in ("fp32_refine", "ff"):
+                with pbt.BtdmaGpuPlan() as pl:
+                    pl.create(M, NSYS, NROW, nseg_m, precision=prec, tol=1e-12, max_iter=8)
+                    ms = time_device(pl, (ma, mb, mc), [md], M, NSYS, NROW, 3, 3, ws, dev, solve)
+                    ms = max_over_ranks(ms, ws, dev)
+                    xo = md.clone()
+                    solve(pl, ma, mb, mc, xo, M, NSYS, NROW)
+                    info = pl.refine_info() if prec == "fp32_refine" else (None, None)
+                entry[prec] = {"block_rows_per_s": ws * mrows * 3 / ms, "ms_per_step": ms / 3 * 1e3,
+                               "rel_err_vs_fp64": rel_err_vs(xo, ref, M, NSYS, NROW)}
+                if prec == "fp32_refine":
+                    entry[prec]["fp32_solves"] = info[0]
+                    entry[prec]["last_correction"] = info[1]
+                del xo
+            mixed[f"delta{delta}_P{nseg_m}"] = entry
+            del ref
+        del ma, mb, mc, md, mw
+        torch.cuda.empty_cache()
+
     result = {
         "metric": "block-rows/s (chosen method at <=1e-10 rel err vs plain FP64)",
         "value": value,
@@ -394,6 +431,7 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "clocks": clocks,
         "variants": variants,
+        "mixed_precision": mixed,
     }
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(m, nrow, nseg, DELTA, target_s=args.cpu_seconds)

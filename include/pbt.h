@@ -75,7 +75,7 @@ typedef enum pbt_status {
 typedef enum pbt_precision {
     PBT_PREC_FP64 = 0,        /* plain FP64 arithmetic, partial-pivot LU per block */
     PBT_PREC_FF = 1,          /* FP64 data, float-float (two-FP32) arithmetic on the FP32 pipes */
-    PBT_PREC_FP32_REFINE = 2  /* FP32 factorisation + FP64-residual iterative refinement */
+    PBT_PREC_FP32_REFINE = 2  /* FP32 factorisation + FP64-residual iterative refinement (non-cyclic) */
 } pbt_precision;
 
 /* Plan flags. */
@@ -179,6 +179,14 @@ int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, double* d,
  * no such report; its dgesv-less GPU path divides by zero silently).  Returns
  * PBT_ESINGULAR when *nsingular > 0.  nsingular may be NULL. */
 int pbt_plan_status(pbt_plan* plan, long long* nsingular);
+
+/* Outcome of the last solve on a PBT_PREC_FP32_REFINE plan: the number of
+ * FP32 solves it ran (the first solve plus the corrections) and the last
+ * correction size, max over systems of max|e| / max|x|.  The refined solve
+ * stops once that size is <= desc.tol (after at least one correction) or
+ * after desc.max_iter solves, and synchronises its stream once per solve to
+ * test it.  Zeros for other precisions.  No counterpart in the reference. */
+int pbt_plan_refine_info(const pbt_plan* plan, int* iterations, double* last_correction);
 
 /* Copies the plan's creation parameters into *desc. */
 int pbt_plan_get_desc(const pbt_plan* plan, pbt_plan_desc* desc);

@@ -174,6 +174,12 @@ class BtdmaGpuPlan:
             _raise(code, "BtdmaGpuPlan.status")
         return int(n.value)
 
+    def refine_info(self) -> tuple[int, float]:
+        """(FP32 solves run, last correction size) of the last refined solve."""
+        it, corr = C.c_int(0), C.c_double(0.0)
+        _raise(N.lib().pbt_plan_refine_info(self._handle, C.byref(it), C.byref(corr)), "refine_info")
+        return it.value, corr.value
+
     def __enter__(self) -> "BtdmaGpuPlan":
         return self
 

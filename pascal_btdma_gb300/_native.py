@@ -74,6 +74,7 @@ SIGNATURES = {
     "pbt_solve_cyclic": (C.c_int, [_P, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, _P]),
     "pbt_solve_noncyclic_noalloc": (C.c_int, [_D, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "pbt_plan_status": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "pbt_plan_refine_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "pbt_plan_get_desc": (C.c_int, [_P, C.POINTER(PlanDesc)]),
     "pbt_plan_workspace_bytes": (C.c_size_t, [_P]),
     "pbt_last_error_string": (C.c_char_p, []),

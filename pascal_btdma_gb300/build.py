@@ -33,7 +33,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 MAX_BLOCK = 10
 
 # Families of kernels instantiated per block size: (source, object stem).
-PER_M_SOURCES = [("pbt_inst.cu", "F64"), ("pbt_inst.cu", "FF")]
+PER_M_SOURCES = [("pbt_inst.cu", "F64"), ("pbt_inst.cu", "FF"), ("pbt_inst.cu", "F32")]
 HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu", "pbt_noalloc.cu"]
 
 
@@ -73,7 +73,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
             obj = BUILD / f"{stem.lower()}_m{m}.o"
             objs.append(obj)
             if _stale(obj, [CSRC / src] + hdrs):
-                tasks.append((obj, [nvcc, *NVCC_FLAGS, f"-DPBT_M={m}", f"-DPBT_NUM=pbt::{stem}", "-c",
+                extra = ["-DPBT_NUM_IS_F64"] if stem == "F64" else []
+                tasks.append((obj, [nvcc, *NVCC_FLAGS, f"-DPBT_M={m}", f"-DPBT_NUM=pbt::{stem}", *extra, "-c",
                                     str(CSRC / src), "-o", str(obj)]))
     for src in HOST_SOURCES:
         obj = BUILD / (Path(src).stem + ".o")

@@ -47,6 +47,13 @@ struct pbt_plan {
     double* rd = nullptr;
     double* re = nullptr;
     unsigned long long* status = nullptr;
+    // Iterative refinement (PBT_PREC_FP32_REFINE): iterate X, correction /
+    // residual E, convergence statistic, and the outcome of the last solve.
+    double* rx = nullptr;
+    double* re_ = nullptr;
+    unsigned* rstat = nullptr;
+    int last_iters = 0;
+    double last_correction = 0.0;
     size_t bytes = 0;
     cudaStream_t last_stream = nullptr;
     unsigned magic = 0x50425450u;  // "PBTP"
@@ -86,13 +93,46 @@ int pick_tpb(const pbt_plan_desc& d, int work_items) {
         default: return cudaErrorInvalidValue;                             \
     }
 
+// Arithmetic of a kernel launch: the plan's precision, except that the
+// refined solve factors in FP32.
+enum Arith { kF64 = 0, kFF = 1, kF32 = 2 };
+
+int arith_of(int precision) {
+    return precision == PBT_PREC_FF ? kFF : (precision == PBT_PREC_FP32_REFINE ? kF32 : kF64);
+}
+
 #define PBT_DISPATCH(NAME, FN)                                             \
-    cudaError_t NAME(int prec, int m, const pbt::SolveArgs& g) {          \
-        if (prec == PBT_PREC_FF) {                                         \
+    cudaError_t NAME(int arith, int m, const pbt::SolveArgs& g) {         \
+        if (arith == kFF) {                                                \
             PBT_DISPATCH_M(pbt::FF, FN)                                    \
+        }                                                                  \
+        if (arith == kF32) {                                               \
+            PBT_DISPATCH_M(pbt::F32, FN)                                   \
         }                                                                  \
         PBT_DISPATCH_M(pbt::F64, FN)                                       \
     }
+
+#define PBT_DISPATCH_PLAIN_M(FN, ...)                                      \
+    switch (m) {                                                           \
+        case 1: return pbt::FN<1>(__VA_ARGS__);                            \
+        case 2: return pbt::FN<2>(__VA_ARGS__);                            \
+        case 3: return pbt::FN<3>(__VA_ARGS__);                            \
+        case 4: return pbt::FN<4>(__VA_ARGS__);                            \
+        case 5: return pbt::FN<5>(__VA_ARGS__);                            \
+        case 6: return pbt::FN<6>(__VA_ARGS__);                            \
+        case 7: return pbt::FN<7>(__VA_ARGS__);                            \
+        case 8: return pbt::FN<8>(__VA_ARGS__);                            \
+        case 9: return pbt::FN<9>(__VA_ARGS__);                            \
+        case 10: return pbt::FN<10>(__VA_ARGS__);                          \
+        default: return cudaErrorInvalidValue;                             \
+    }
+
+cudaError_t run_residual(int m, const pbt::SolveArgs& g, const double* X, double* E) {
+    PBT_DISPATCH_PLAIN_M(launch_residual, g, X, E)
+}
+cudaError_t run_accumulate(int m, const pbt::SolveArgs& g, double* X, const double* E, unsigned* stat) {
+    PBT_DISPATCH_PLAIN_M(launch_accumulate, g, X, E, stat)
+}
 
 PBT_DISPATCH(run_thomas, launch_thomas)
 PBT_DISPATCH(run_modi, launch_modi)
@@ -127,8 +167,17 @@ int validate(const pbt_plan_desc& d) {
     if ((d.flags & PBT_FLAG_CYCLIC) && d.nseg < 2) {
         return fail(PBT_EINVAL, "plan: the cyclic solve needs nseg >= 2 (a reduced system of at least 4 rows)");
     }
-    if (d.precision != PBT_PREC_FP64 && d.precision != PBT_PREC_FF) {
-        return fail(PBT_EUNSUPPORTED, "plan: precision not provided by this build (FP64 and FF are)");
+    if (d.precision != PBT_PREC_FP64 && d.precision != PBT_PREC_FF && d.precision != PBT_PREC_FP32_REFINE) {
+        return fail(PBT_EUNSUPPORTED, "plan: unknown precision");
+    }
+    if (d.precision == PBT_PREC_FP32_REFINE) {
+        if (d.flags & PBT_FLAG_INPLACE)
+            return fail(PBT_EINVAL, "plan: the refined solve needs A and C unchanged for its FP64 residual "
+                                    "(PBT_FLAG_INPLACE not allowed with PBT_PREC_FP32_REFINE)");
+        if (d.flags & PBT_FLAG_CYCLIC)
+            return fail(PBT_EUNSUPPORTED, "plan: PBT_PREC_FP32_REFINE is provided for non-cyclic lines only");
+        if (!(d.tol > 0.0) || d.max_iter < 1 || d.max_iter > 100)
+            return fail(PBT_EINVAL, "plan: refinement needs tol > 0 and 1 <= max_iter <= 100");
     }
     if (d.threads_per_block != 0 &&
         (d.threads_per_block < 32 || d.threads_per_block > 128 || d.threads_per_block % 32 != 0)) {
@@ -140,6 +189,11 @@ int validate(const pbt_plan_desc& d) {
 }
 
 void free_plan(pbt_plan* p) {
+    cudaFree(p->rx);
+    cudaFree(p->re_);
+    cudaFree(p->rstat);
+    p->rx = p->re_ = nullptr;
+    p->rstat = nullptr;
     cudaFree(p->aw);
     cudaFree(p->cw);
     cudaFree(p->ra);
@@ -204,6 +258,52 @@ struct EventSet {
     }
 };
 
+// The refined solve: x = 0, r = d; repeat { solve M e = r with FP32
+// arithmetic (same kernels, F32); x += e; stop when max over systems of
+// max|e|/max|x| <= tol or after max_iter corrections; r = d - M x in FP64 }.
+// Synchronises the stream once per correction to test convergence.
+int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaStream_t s) {
+    const pbt_plan_desc& ds = p->desc;
+    const int m = ds.m;
+    const size_t nv = (size_t)ds.nsys * ds.nrow * ds.m;
+    cudaError_t e = cudaMemcpyAsync(p->re_, d, nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->rx, 0, nv * sizeof(double), s);
+    if (e != cudaSuccess) return cuda_fail(e, "refined solve: set-up copies");
+    p->last_iters = 0;
+    p->last_correction = 0.0;
+    const pbt::SolveArgs g64 = make_args(p, a, b, c, d, s, ds.nsys);
+    for (int it = 0; it < ds.max_iter; ++it) {
+        if (p->thomas) {
+            e = run_thomas(kF32, m, make_args(p, a, b, c, p->re_, s, ds.nsys));
+        } else {
+            pbt::SolveArgs g = make_args(p, a, b, c, p->re_, s, ds.nsys * ds.nseg);
+            e = run_modi(kF32, m, g);
+            if (e == cudaSuccess) e = run_reduced(kF32, m, make_args(p, a, b, c, p->re_, s, ds.nsys));
+            if (e == cudaSuccess) e = run_update(kF32, m, g);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "refined solve: FP32 correction launch");
+        if ((e = cudaMemsetAsync(p->rstat, 0, sizeof(unsigned), s)) != cudaSuccess)
+            return cuda_fail(e, "refined solve: statistic reset");
+        if ((e = run_accumulate(m, g64, p->rx, p->re_, p->rstat)) != cudaSuccess)
+            return cuda_fail(e, "refined solve: accumulate launch");
+        unsigned bits = 0;
+        if ((e = cudaMemcpyAsync(&bits, p->rstat, sizeof bits, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(s)) != cudaSuccess)
+            return cuda_fail(e, "refined solve: convergence read");
+        float ratio;
+        std::memcpy(&ratio, &bits, sizeof ratio);
+        p->last_iters = it + 1;
+        p->last_correction = ratio;
+        if (it > 0 && ratio <= ds.tol) break;
+        if (it + 1 == ds.max_iter) break;
+        if ((e = run_residual(m, g64, p->rx, p->re_)) != cudaSuccess)
+            return cuda_fail(e, "refined solve: residual launch");
+    }
+    e = cudaMemcpyAsync(d, p->rx, nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "refined solve: result copy");
+    return PBT_OK;
+}
+
 int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow,
                bool cyclic, pbt_timings* t, void* stream) {
     int rc = check_plan(p);
@@ -230,22 +330,27 @@ int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
 
     cudaError_t e;
     if ((e = mark(0)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
-    if (p->thomas) {
-        e = run_thomas(ds.precision, m, make_args(p, a, b, c, d, s, nsys));
+    if (ds.precision == PBT_PREC_FP32_REFINE) {
+        rc = solve_refined(p, a, b, c, d, s);
+        if (rc) return rc;
+        for (int i = 1; i < 5; ++i)
+            if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    } else if (p->thomas) {
+        e = run_thomas(arith_of(ds.precision), m, make_args(p, a, b, c, d, s, nsys));
         if (e != cudaSuccess) return cuda_fail(e, "block Thomas launch");
         for (int i = 1; i < 5; ++i)
             if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     } else {
         pbt::SolveArgs g = make_args(p, a, b, c, d, s, nsys * ds.nseg);
-        e = run_modi(ds.precision, m, g);
+        e = run_modi(arith_of(ds.precision), m, g);
         if (e != cudaSuccess) return cuda_fail(e, "local-stage launch");
         if ((e = mark(1)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
         if ((e = mark(2)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
         pbt::SolveArgs g2 = make_args(p, a, b, c, d, s, nsys);
-        e = cyclic ? run_reduced_cyclic(ds.precision, m, g2) : run_reduced(ds.precision, m, g2);
+        e = cyclic ? run_reduced_cyclic(arith_of(ds.precision), m, g2) : run_reduced(arith_of(ds.precision), m, g2);
         if (e != cudaSuccess) return cuda_fail(e, "reduced-stage launch");
         if ((e = mark(3)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
-        e = run_update(ds.precision, m, g);
+        e = run_update(arith_of(ds.precision), m, g);
         if (e != cudaSuccess) return cuda_fail(e, "update-stage launch");
         if ((e = mark(4)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     }
@@ -311,6 +416,16 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
         if ((rc = alloc(p, &p->rc, mm * rrows))) goto fail_out;
         if ((rc = alloc(p, &p->rd, (size_t)d.m * rrows))) goto fail_out;
         if (cyclic && (rc = alloc(p, &p->re, mm * rrows))) goto fail_out;
+    }
+    if (d.precision == PBT_PREC_FP32_REFINE) {
+        const size_t nv = (size_t)d.m * rows;
+        if ((rc = alloc(p, &p->rx, nv))) goto fail_out;
+        if ((rc = alloc(p, &p->re_, nv))) goto fail_out;
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->rstat), sizeof(unsigned));
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "plan_create: refinement statistic");
+            goto fail_out;
+        }
     }
     {
         cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->status), sizeof(unsigned long long));
@@ -380,6 +495,14 @@ int pbt_plan_status(pbt_plan* p, long long* nsingular) {
     if (e != cudaSuccess) return cuda_fail(e, "plan_status: reset");
     if (nsingular) *nsingular = (long long)v;
     if (v) return fail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
+    return PBT_OK;
+}
+
+int pbt_plan_refine_info(const pbt_plan* p, int* iterations, double* last_correction) {
+    int rc = check_plan(p);
+    if (rc) return rc;
+    if (iterations) *iterations = p->last_iters;
+    if (last_correction) *last_correction = p->last_correction;
     return PBT_OK;
 }
 

@@ -1,6 +1,6 @@
 // pbt_inst.cu -- explicit instantiation of the solver kernels for one
 // arithmetic and one block size.  The build compiles this file once per
-// (PBT_NUM, PBT_M), PBT_NUM in {F64, FF} and PBT_M in 1..PBT_MAX_BLOCK, so the
+// (PBT_NUM, PBT_M), PBT_NUM in {F64, FF, F32} and PBT_M in 1..PBT_MAX_BLOCK, so the
 // unrolled variants compile in parallel.
 #if !defined(PBT_M) || !defined(PBT_NUM)
 #error "compile with -DPBT_M=<block size> -DPBT_NUM=<F64|FF>"
@@ -18,4 +18,8 @@ template cudaError_t launch_modi<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_reduced<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_reduced_cyclic<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_update<PBT_NUM, PBT_M>(const SolveArgs&);
+#ifdef PBT_NUM_IS_F64
+template cudaError_t launch_residual<PBT_M>(const SolveArgs&, const double*, double*);
+template cudaError_t launch_accumulate<PBT_M>(const SolveArgs&, double*, const double*, unsigned*);
+#endif
 }  // namespace pbt

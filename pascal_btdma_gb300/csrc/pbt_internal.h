@@ -34,9 +34,10 @@ struct SolveArgs {
     cudaStream_t stream;
 };
 
-// The two arithmetics of pbt_num.cuh.
+// The arithmetics of pbt_num.cuh.
 struct F64;
 struct FF;
+struct F32;
 
 // Kernel launchers, explicitly instantiated per arithmetic and block size M
 // (1..PBT_MAX_BLOCK) in pbt_inst.cu.  Each returns cudaGetLastError().
@@ -45,6 +46,9 @@ template <class Num, int M> cudaError_t launch_modi(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced_cyclic(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_update(const SolveArgs& g);
+// FP64 parts of the refined solve (instantiated with the F64 kernels).
+template <int M> cudaError_t launch_residual(const SolveArgs& g, const double* X, double* E);
+template <int M> cudaError_t launch_accumulate(const SolveArgs& g, double* X, const double* E, unsigned* stat);
 
 // Records the message returned by pbt_last_error_string() on this thread and
 // returns `code` (defined in pbt_api.cpp).

@@ -186,7 +186,7 @@ PBT_UNROLL
 // Factor storage: raw in the plan's workspace, FP64 when written in place.
 template <class Num, int M>
 __device__ __forceinline__ void st_fac_blk(double* base, size_t plane, const typename Num::T (&x)[M][M], bool raw) {
-    if (raw || !Num::kIsFF) {
+    if (raw || !Num::kConv) {
         st_raw_blk<Num, M>(base, plane, x);
     } else {
 PBT_UNROLL
@@ -197,7 +197,7 @@ PBT_UNROLL
 }
 template <class Num, int M>
 __device__ __forceinline__ void ld_fac_blk(typename Num::T (&x)[M][M], const double* base, size_t plane, bool raw) {
-    if (raw || !Num::kIsFF)
+    if (raw || !Num::kConv)
         ld_raw_blk<Num, M>(x, base, plane);
     else
         in_blk<Num, M>(x, base, plane);
@@ -529,7 +529,7 @@ PBT_UNROLL
 PBT_UNROLL
         for (int i = 0; i < M; ++i) {
             T c0[M];
-            if (raw || !Num::kIsFF) {
+            if (raw || !Num::kConv) {
 PBT_UNROLL
                 for (int k = 0; k < M; ++k) c0[k] = Num::lds(CW + (size_t)(i + M * k) * plane);
             } else {
@@ -559,7 +559,7 @@ PBT_UNROLL
 PBT_UNROLL
             for (int j = 0; j < M; ++j) {
                 const double* p = AW + (size_t)(i + M * j) * plane;
-                x[i][j] = Num::acc((raw || !Num::kIsFF) ? Num::lds(p) : Num::in(p));
+                x[i][j] = Num::acc((raw || !Num::kConv) ? Num::lds(p) : Num::in(p));
             }
         gesv<Num, M, 2 * M + 1>(r, x, bad);
 PBT_UNROLL
@@ -885,6 +885,82 @@ PBT_UNROLL
 }
 
 // ---------------------------------------------------------------------------
+// Iterative refinement (precision PBT_PREC_FP32_REFINE), FP64 parts.
+//   k_residual64: E = d - M X for every system, in FP64 (the one FP64 pass of
+//                 the refined solve): r_q = d_q - A_q x_{q-1} - B_q x_q - C_q x_{q+1}
+//                 (A_0 and C_{N-1} not read, as in the non-cyclic solve).
+//   k_accumulate: X += E, and the largest max|E| / max|X| over the systems
+//                 into *stat (as ordered float bits) for the convergence test.
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(128) k_residual64(const SolveArgs g, const double* __restrict__ X,
+                                                   double* __restrict__ E) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int N = g.nrow;
+    const size_t plane0 = (size_t)g.nsys * N;
+    const size_t rs = (size_t)g.nsys;
+    double xm[M], x0[M], xp[M];
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) {
+        xm[i] = 0.0;
+        x0[i] = X[sys + (size_t)i * plane0];
+    }
+    for (int q = 0; q < N; ++q) {
+        const size_t o = (size_t)q * rs + sys;
+        const size_t plane = opaque(plane0);
+        const bool has_next = (q + 1 < N);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) xp[i] = has_next ? X[o + rs + (size_t)i * plane] : 0.0;
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            double t = __ldg(g.d + o + (size_t)i * plane);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) t = fma(-__ldg(g.b + o + (size_t)(i + M * k) * plane), x0[k], t);
+            if (q > 0) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) t = fma(-__ldg(g.a + o + (size_t)(i + M * k) * plane), xm[k], t);
+            }
+            if (has_next) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) t = fma(-__ldg(g.c + o + (size_t)(i + M * k) * plane), xp[k], t);
+            }
+            E[o + (size_t)i * plane] = t;
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            xm[i] = x0[i];
+            x0[i] = xp[i];
+        }
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__(128) k_accumulate(const SolveArgs g, double* __restrict__ X,
+                                                   const double* __restrict__ E, unsigned* stat) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const size_t plane0 = (size_t)g.nsys * g.nrow;
+    const size_t rs = (size_t)g.nsys;
+    double emax = 0.0, xmax = 0.0;
+    for (int q = 0; q < g.nrow; ++q) {
+        const size_t o = (size_t)q * rs + sys;
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            const double e = E[o + (size_t)i * plane0];
+            const double x = X[o + (size_t)i * plane0] + e;
+            X[o + (size_t)i * plane0] = x;
+            emax = fmax(emax, fabs(e));
+            xmax = fmax(xmax, fabs(x));
+        }
+    }
+    // NaN-safe: a non-finite or undefined ratio reports +Inf.
+    float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
+    if (!(ratio == ratio)) ratio = INFINITY;
+    atomicMax(stat, __float_as_uint(ratio));
+}
+
+// ---------------------------------------------------------------------------
 // Launchers.
 // ---------------------------------------------------------------------------
 inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) / tpb); }
@@ -909,6 +985,16 @@ cudaError_t launch_reduced(const SolveArgs& g) {
 template <class Num, int M>
 cudaError_t launch_reduced_cyclic(const SolveArgs& g) {
     k_reduced_cyclic<Num, M><<<grid_x(g.nsys, g.tpb), g.tpb, 0, g.stream>>>(g);
+    return cudaGetLastError();
+}
+template <int M>
+cudaError_t launch_residual(const SolveArgs& g, const double* X, double* E) {
+    k_residual64<M><<<grid_x(g.nsys, 128), 128, 0, g.stream>>>(g, X, E);
+    return cudaGetLastError();
+}
+template <int M>
+cudaError_t launch_accumulate(const SolveArgs& g, double* X, const double* E, unsigned* stat) {
+    k_accumulate<M><<<grid_x(g.nsys, 128), 128, 0, g.stream>>>(g, X, E, stat);
     return cudaGetLastError();
 }
 template <class Num, int M>

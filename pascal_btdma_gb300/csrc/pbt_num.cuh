@@ -1,4 +1,4 @@
-// pbt_num.cuh -- the two arithmetics the solver kernels are written over.
+// pbt_num.cuh -- the arithmetics the solver kernels are written over.
 //
 //   F64: plain IEEE double on the FP64 pipe (1/63 of the FP32 rate on GB300).
 //   FF:  float-float ("double-single") arithmetic on the FP32 pipes.  A value
@@ -9,6 +9,8 @@
 //        Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).
 //        Each multiply-accumulate costs 12 FP32 instructions, i.e. ~5x the
 //        FP64 pipe's rate.
+//   F32: plain float, the factorisation arithmetic of the iteratively refined
+//        solve (see k_residual64 in pbt_kernels.cuh).
 //
 // Every kernel uses the same small interface:
 //   T            register value;  Acc: an accumulator for sums of products
@@ -48,7 +50,7 @@ struct F64 {
     struct Acc {
         double v;
     };
-    static constexpr bool kIsFF = false;
+    static constexpr bool kConv = false;  // raw workspace values differ from FP64?
 
     __device__ static __forceinline__ T in(const double* p) { return *p; }
     __device__ static __forceinline__ T in_ro(const double* p) { return __ldg(p); }
@@ -98,7 +100,7 @@ struct FF {
     struct Acc {
         float s, t;  // unnormalised: value = s + t, t collects rounding errors and low parts
     };
-    static constexpr bool kIsFF = true;
+    static constexpr bool kConv = true;
 
     // FP64 -> (h, l) by bit manipulation: h = x truncated to 24 significant
     // bits, l = the next 23 bits.  |x - (h + l)| < 2^-46 |x| for
@@ -177,6 +179,41 @@ struct FF {
     __device__ static __forceinline__ Acc asel(unsigned s, Acc x, Acc y) { return {fsel(s, x.s, y.s), fsel(s, x.t, y.t)}; }
     // Pivot key of an accumulator: its high part decides.
     __device__ static __forceinline__ unsigned akey(Acc a) { return __float_as_uint(a.s) & 0x7fffffffu; }
+    __device__ static __forceinline__ bool is_zero(T a) { return key(a) == 0u; }
+};
+
+// ---------------------------------------------------------------------------
+// F32: plain IEEE float, for the FP32 factorisation of the refined solve.
+// Inputs are rounded to float on load; raw workspace slots (8 bytes) hold the
+// float in their first 4 bytes.
+struct F32 {
+    using T = float;
+    struct Acc {
+        float v;
+    };
+    static constexpr bool kConv = true;
+
+    __device__ static __forceinline__ T in(const double* p) { return __double2float_rn(*p); }
+    __device__ static __forceinline__ T in_ro(const double* p) { return __double2float_rn(__ldg(p)); }
+    __device__ static __forceinline__ void out(double* p, T v) { *p = static_cast<double>(v); }
+    __device__ static __forceinline__ T lds(const double* p) { return *reinterpret_cast<const float*>(p); }
+    __device__ static __forceinline__ void sts(double* p, T v) { *reinterpret_cast<float*>(p) = v; }
+
+    __device__ static __forceinline__ Acc acc(T x) { return {x}; }
+    __device__ static __forceinline__ Acc acc0() { return {0.f}; }
+    __device__ static __forceinline__ void mac(Acc& a, T x, T y) { a.v = __fmaf_rn(x, y, a.v); }
+    __device__ static __forceinline__ void msub(Acc& a, T x, T y) { a.v = __fmaf_rn(-x, y, a.v); }
+    __device__ static __forceinline__ T fin(Acc a) { return a.v; }
+
+    __device__ static __forceinline__ T mul(T a, T b) { return __fmul_rn(a, b); }
+    __device__ static __forceinline__ T rcp(T a) { return __frcp_rn(a); }
+    __device__ static __forceinline__ T neg(T a) { return -a; }
+    __device__ static __forceinline__ T zero() { return 0.f; }
+    __device__ static __forceinline__ T one() { return 1.f; }
+    __device__ static __forceinline__ unsigned key(T a) { return __float_as_uint(a) & 0x7fffffffu; }
+    __device__ static __forceinline__ T sel(unsigned s, T x, T y) { return fsel(s, x, y); }
+    __device__ static __forceinline__ Acc asel(unsigned s, Acc x, Acc y) { return {fsel(s, x.v, y.v)}; }
+    __device__ static __forceinline__ unsigned akey(Acc a) { return key(a.v); }
     __device__ static __forceinline__ bool is_zero(T a) { return key(a) == 0u; }
 };
 

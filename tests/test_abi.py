@@ -77,6 +77,9 @@ def create(**kw):
         (dict(flags=0x100), N.PBT_EINVAL, "unknown flag"),
         (dict(threads_per_block=48), N.PBT_EINVAL, "threads_per_block"),
         (dict(precision=7), N.PBT_EUNSUPPORTED, "precision"),
+        (dict(precision=N.PBT_PREC_FP32_REFINE, flags=N.PBT_FLAG_INPLACE), N.PBT_EINVAL, "unchanged"),
+        (dict(precision=N.PBT_PREC_FP32_REFINE, nseg=2, flags=N.PBT_FLAG_CYCLIC), N.PBT_EUNSUPPORTED, "non-cyclic"),
+        (dict(precision=N.PBT_PREC_FP32_REFINE, max_iter=0), N.PBT_EINVAL, "max_iter"),
     ],
 )
 def test_plan_create_rejects(kw, code, msg):

@@ -188,3 +188,52 @@ def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta):
         print(f"{prec} m={m} nsys={nsys} nrow={nrow} nseg={nseg}: max rel err {err:.3e}")
         assert err <= tol
         assert np.isfinite(D).all()
+
+
+REFINE_TOL = 1e-10  # the mixed-precision target: FP32 factorisation + FP64 residual refinement
+
+
+@pytest.mark.parametrize("m,nsys,nrow,nseg", [(1, 37, 12, 4), (2, 65, 9, 1), (3, 33, 12, 4), (4, 31, 40, 8),
+                                              (5, 70, 24, 3), (5, 64, 256, 16), (6, 17, 18, 6), (8, 20, 16, 5),
+                                              (10, 7, 30, 3), (4, 300, 128, 1)])
+@pytest.mark.parametrize("delta", [1.05, 2.0])
+def test_refined_matches_oracle(cuda, m, nsys, nrow, nseg, delta):
+    w = synth.dominant(m, nsys, nrow, seed=2000 * m + nseg, delta=delta)
+    a, b, c, d = to_dev(w.arrays, cuda)
+    with pbt.BtdmaGpuPlan() as plan:
+        plan.create(m, nsys, nrow, nseg, precision="fp32_refine")
+        pbt.solve_noncyclic(plan, a, b, c, d, m, nsys, nrow)
+        iters, corr = plan.refine_info()
+    ref = oracle_solve(w, nseg)
+    err = per_system_relerr(m, nsys, nrow, d.cpu().numpy(), ref.D)
+    assert err <= REFINE_TOL
+    assert 2 <= iters <= 8 and corr <= 1e-12
+    assert torch.equal(a.cpu(), torch.from_numpy(w.A)) and torch.equal(c.cpu(), torch.from_numpy(w.C))
+
+
+@pytest.mark.parametrize("delta", [1.05, 1.5])
+@pytest.mark.parametrize("nseg", [1, 16])
+def test_refined_row_scaled(cuda, delta, nseg):
+    """The mixed-precision configuration, fewer systems: m=5, N=256, each block
+    row scaled by a log-uniform factor in [1e-3, 1e3]."""
+    m, nsys, nrow = 5, 512, 256
+    w = synth.dominant(m, nsys, nrow, seed=44, delta=delta, row_scale=True)
+    a, b, c, d = to_dev(w.arrays, cuda)
+    with pbt.BtdmaGpuPlan() as plan:
+        plan.create(m, nsys, nrow, nseg, precision="fp32_refine")
+        pbt.solve_noncyclic(plan, a, b, c, d, m, nsys, nrow)
+        iters, corr = plan.refine_info()
+    ref = oracle_solve(w, nseg)
+    err = per_system_relerr(m, nsys, nrow, d.cpu().numpy(), ref.D)
+    print(f"refined delta={delta} nseg={nseg}: {iters} FP32 solves, last correction {corr:.2e}, rel err {err:.2e}")
+    assert err <= REFINE_TOL
+
+
+def test_refine_stops_at_max_iter(cuda):
+    w = synth.dominant(3, 64, 40, seed=5, delta=1.05)
+    a, b, c, d = to_dev(w.arrays, cuda)
+    with pbt.BtdmaGpuPlan() as plan:
+        plan.create(3, 64, 40, 1, precision="fp32_refine", tol=1e-30, max_iter=3)
+        pbt.solve_noncyclic(plan, a, b, c, d, 3, 64, 40)
+        iters, corr = plan.refine_info()
+    assert iters == 3 and corr > 0
