@@ -174,6 +174,22 @@ int pbt_solve_cyclic(pbt_plan* plan, double* a, double* b, double* c, double* d,
 int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, double* d,
                                 int m, int nsys, int nrow, int nseg, void* stream);
 
+/* Adjoint of the non-cyclic solve x = M^{-1} d (no counterpart in the
+ * reference).  On entry g holds dL/dx for a scalar loss L; on return it holds
+ * lambda = M^{-T} dL/dx = dL/dd, and da, db, dc (each nsys*nrow*m*m doubles,
+ * reference layout; any may be NULL) receive
+ *   dL/dA_q = -lambda_q x_{q-1}^T,  dL/dB_q = -lambda_q x_q^T,  dL/dC_q = -lambda_q x_{q+1}^T,
+ * with dL/dA_0 = dL/dC_{nrow-1} = 0.  x is the forward solution and a, b, c
+ * the forward blocks, unchanged (the plan must not be PBT_FLAG_INPLACE).
+ * nseg = 1, m <= 6: one fused kernel solves M^T lambda = g by block Thomas
+ * on the transposed blocks, read in place, and forms the gradient blocks in
+ * its backward sweep.  Otherwise M^T's blocks are materialised in plan
+ * workspace (allocated by the first such call), solved by the plan's forward
+ * method, and the gradients formed in one more pass.  Precision fp64 or ff. */
+int pbt_adjoint_noncyclic(pbt_plan* plan, const double* a, const double* b, const double* c,
+                          const double* x, double* g, double* da, double* db, double* dc,
+                          int m, int nsys, int nrow, void* stream);
+
 /* Synchronises the plan's last stream and reports through *nsingular how
  * many zero pivots the solves since the previous call met (the reference has
  * no such report; its dgesv-less GPU path divides by zero silently).  Returns
@@ -182,10 +198,11 @@ int pbt_plan_status(pbt_plan* plan, long long* nsingular);
 
 /* Outcome of the last solve on a PBT_PREC_FP32_REFINE plan: the number of
  * FP32 solves it ran (the first solve plus the corrections) and the last
- * correction size, max over systems of max|e| / max|x|.  The refined solve
- * stops once that size is <= desc.tol (after at least one correction) or
- * after desc.max_iter solves, and synchronises its stream once per solve to
- * test it.  Zeros for other precisions.  No counterpart in the reference. */
+ * correction size c_k = max over systems of max|e| / max|x|.  The refined
+ * solve stops once the estimated remaining error c_k^2 / c_{k-1} (c_0 = 1,
+ * the first solve) is <= desc.tol, or after desc.max_iter solves, and
+ * synchronises its stream once per solve to test it.  Zeros for other
+ * precisions.  No counterpart in the reference. */
 int pbt_plan_refine_info(const pbt_plan* plan, int* iterations, double* last_correction);
 
 /* Copies the plan's creation parameters into *desc. */

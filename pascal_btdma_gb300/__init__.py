@@ -41,6 +41,8 @@ __all__ = [
     "solve_noncyclic",
     "solve_noncyclic_profiled",
     "solve_cyclic",
+    "adjoint_noncyclic",
+    "BlockTridiagonalSolve",
     "partition_1d",
     "matrix_index",
     "vector_index",
@@ -280,3 +282,62 @@ def matrix_index(sys: int, row: int, p: int, q: int, nsys: int, nrow: int, m: in
 def vector_index(sys: int, row: int, p: int, nsys: int, nrow: int) -> int:
     """Element p of vector (sys, row) (pascal_btdma_cuda.hpp:58-65)."""
     return sys + nsys * (row + nrow * p)
+
+
+def adjoint_noncyclic(plan, a, b, c, x, g, da=None, db=None, dc=None, m=None, nsys=None, nrow=None, stream=None) -> None:
+    """Adjoint of the non-cyclic solve: g (dL/dx) <- lambda = dL/dd; da, db, dc
+    (optional) <- dL/dA, dL/dB, dL/dC.  a, b, c, x are the forward blocks and
+    solution, unchanged."""
+    if not isinstance(plan, BtdmaGpuPlan) or not plan.created:
+        raise RuntimeError("adjoint_noncyclic called with an uncreated BtdmaGpuPlan")
+    m = plan.m if m is None else m
+    nsys = plan.nsys if nsys is None else nsys
+    nrow = plan.nrow if nrow is None else nrow
+    arrays = (a, b, c, x, g) + tuple(t for t in (da, db, dc) if t is not None)
+    s = _stream(stream, arrays)
+    opt = [C.c_void_p(_ptr(t)) if t is not None else None for t in (da, db, dc)]
+    code = N.lib().pbt_adjoint_noncyclic(plan.handle, *(C.c_void_p(_ptr(t)) for t in (a, b, c, x, g)), *opt,
+                                         int(m), int(nsys), int(nrow), C.c_void_p(s))
+    _raise(code, "adjoint_noncyclic")
+
+
+def _autograd_function():
+    import torch
+
+    class _Solve(torch.autograd.Function):
+        """x = M^{-1} d for the batched block-tridiagonal M given by (A, B, C),
+        differentiable in A, B, C and d through the hand-written adjoint."""
+
+        @staticmethod
+        def forward(ctx, A, B, C, d, plan):
+            x = d.detach().clone()
+            solve_noncyclic(plan, A.detach(), B.detach(), C.detach(), x, plan.m, plan.nsys, plan.nrow)
+            ctx.plan = plan
+            ctx.save_for_backward(A, B, C, x)
+            return x
+
+        @staticmethod
+        def backward(ctx, grad_x):
+            A, B, C, x = ctx.saved_tensors
+            plan = ctx.plan
+            lam = grad_x.detach().clone().contiguous()
+            need = ctx.needs_input_grad
+            dA = torch.empty_like(A) if need[0] else None
+            dB = torch.empty_like(B) if need[1] else None
+            dC = torch.empty_like(C) if need[2] else None
+            adjoint_noncyclic(plan, A.detach(), B.detach(), C.detach(), x, lam, dA, dB, dC)
+            return dA, dB, dC, (lam if need[3] else None), None
+
+    return _Solve
+
+
+class _LazySolve:
+    _fn = None
+
+    def apply(self, A, B, C, d, plan):
+        if _LazySolve._fn is None:
+            _LazySolve._fn = _autograd_function()
+        return _LazySolve._fn.apply(A, B, C, d, plan)
+
+
+BlockTridiagonalSolve = _LazySolve()

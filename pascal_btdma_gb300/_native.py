@@ -72,6 +72,10 @@ SIGNATURES = {
         [_P, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.POINTER(Timings), _P],
     ),
     "pbt_solve_cyclic": (C.c_int, [_P, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, _P]),
+    "pbt_adjoint_noncyclic": (
+        C.c_int,
+        [_P, _D, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, _P],
+    ),
     "pbt_solve_noncyclic_noalloc": (C.c_int, [_D, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "pbt_plan_status": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "pbt_plan_refine_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),

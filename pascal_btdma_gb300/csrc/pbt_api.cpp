@@ -51,6 +51,10 @@ struct pbt_plan {
     // residual E, convergence statistic, and the outcome of the last solve.
     double* rx = nullptr;
     double* re_ = nullptr;
+    // Adjoint of a segmented plan: M^T's blocks, allocated on first use.
+    double* at = nullptr;
+    double* bt = nullptr;
+    double* ct = nullptr;
     unsigned* rstat = nullptr;
     int last_iters = 0;
     double last_correction = 0.0;
@@ -112,6 +116,21 @@ int arith_of(int precision) {
         PBT_DISPATCH_M(pbt::F64, FN)                                       \
     }
 
+#define PBT_DISPATCH_PLAIN_M2(NUM, FN, ...)                                \
+    switch (m) {                                                           \
+        case 1: return pbt::FN<NUM, 1>(__VA_ARGS__);                       \
+        case 2: return pbt::FN<NUM, 2>(__VA_ARGS__);                       \
+        case 3: return pbt::FN<NUM, 3>(__VA_ARGS__);                       \
+        case 4: return pbt::FN<NUM, 4>(__VA_ARGS__);                       \
+        case 5: return pbt::FN<NUM, 5>(__VA_ARGS__);                       \
+        case 6: return pbt::FN<NUM, 6>(__VA_ARGS__);                       \
+        case 7: return pbt::FN<NUM, 7>(__VA_ARGS__);                       \
+        case 8: return pbt::FN<NUM, 8>(__VA_ARGS__);                       \
+        case 9: return pbt::FN<NUM, 9>(__VA_ARGS__);                       \
+        case 10: return pbt::FN<NUM, 10>(__VA_ARGS__);                     \
+        default: return cudaErrorInvalidValue;                             \
+    }
+
 #define PBT_DISPATCH_PLAIN_M(FN, ...)                                      \
     switch (m) {                                                           \
         case 1: return pbt::FN<1>(__VA_ARGS__);                            \
@@ -127,6 +146,18 @@ int arith_of(int precision) {
         default: return cudaErrorInvalidValue;                             \
     }
 
+cudaError_t run_adjoint(int arith, int m, const pbt::SolveArgs& g, const pbt::AdjointArgs& adj) {
+    if (arith == kFF) {
+        PBT_DISPATCH_PLAIN_M2(pbt::FF, launch_adjoint, g, adj)
+    }
+    PBT_DISPATCH_PLAIN_M2(pbt::F64, launch_adjoint, g, adj)
+}
+cudaError_t run_transpose_blocks(int m, const pbt::SolveArgs& g, double* At, double* Bt, double* Ct) {
+    PBT_DISPATCH_PLAIN_M(launch_transpose_blocks, g, At, Bt, Ct)
+}
+cudaError_t run_gradients(int m, const pbt::SolveArgs& g, const pbt::AdjointArgs& adj) {
+    PBT_DISPATCH_PLAIN_M(launch_gradients, g, adj)
+}
 cudaError_t run_residual(int m, const pbt::SolveArgs& g, const double* X, double* E) {
     PBT_DISPATCH_PLAIN_M(launch_residual, g, X, E)
 }
@@ -189,6 +220,10 @@ int validate(const pbt_plan_desc& d) {
 }
 
 void free_plan(pbt_plan* p) {
+    cudaFree(p->at);
+    cudaFree(p->bt);
+    cudaFree(p->ct);
+    p->at = p->bt = p->ct = nullptr;
     cudaFree(p->rx);
     cudaFree(p->re_);
     cudaFree(p->rstat);
@@ -259,9 +294,10 @@ struct EventSet {
 };
 
 // The refined solve: x = 0, r = d; repeat { solve M e = r with FP32
-// arithmetic (same kernels, F32); x += e; stop when max over systems of
-// max|e|/max|x| <= tol or after max_iter corrections; r = d - M x in FP64 }.
-// Synchronises the stream once per correction to test convergence.
+// arithmetic (same kernels, F32); x += e; stop when the estimated remaining
+// error, c_k^2 / c_{k-1} with c_k = max over systems of max|e|/max|x| (and
+// c_0 = 1), is <= tol, or after max_iter FP32 solves; r = d - M x in FP64 }.
+// Synchronises the stream once per FP32 solve to test convergence.
 int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaStream_t s) {
     const pbt_plan_desc& ds = p->desc;
     const int m = ds.m;
@@ -272,6 +308,7 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
     p->last_iters = 0;
     p->last_correction = 0.0;
     const pbt::SolveArgs g64 = make_args(p, a, b, c, d, s, ds.nsys);
+    double prev_ratio = 1.0;
     for (int it = 0; it < ds.max_iter; ++it) {
         if (p->thomas) {
             e = run_thomas(kF32, m, make_args(p, a, b, c, p->re_, s, ds.nsys));
@@ -294,7 +331,11 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
         std::memcpy(&ratio, &bits, sizeof ratio);
         p->last_iters = it + 1;
         p->last_correction = ratio;
-        if (it > 0 && ratio <= ds.tol) break;
+        // Stop when the estimated error left after this correction,
+        // ratio * rho with the contraction rho = ratio / previous ratio
+        // (the first solve counts as a correction of size 1), is below tol.
+        if (it > 0 && (double)ratio * ((double)ratio / prev_ratio) <= ds.tol) break;
+        prev_ratio = ratio > 0.f ? (double)ratio : 1e-300;
         if (it + 1 == ds.max_iter) break;
         if ((e = run_residual(m, g64, p->rx, p->re_)) != cudaSuccess)
             return cuda_fail(e, "refined solve: residual launch");
@@ -495,6 +536,63 @@ int pbt_plan_status(pbt_plan* p, long long* nsingular) {
     if (e != cudaSuccess) return cuda_fail(e, "plan_status: reset");
     if (nsingular) *nsingular = (long long)v;
     if (v) return fail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
+    return PBT_OK;
+}
+
+int pbt_adjoint_noncyclic(pbt_plan* p, const double* a, const double* b, const double* c, const double* x,
+                          double* g, double* da, double* db, double* dc, int m, int nsys, int nrow, void* stream) {
+    int rc = check_plan(p);
+    if (rc) return rc;
+    const pbt_plan_desc& ds = p->desc;
+    if (m != ds.m || nsys != ds.nsys || nrow != ds.nrow) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "adjoint dimensions (m=%d, nsys=%d, nrow=%d) do not match the plan (%d, %d, %d)",
+                      m, nsys, nrow, ds.m, ds.nsys, ds.nrow);
+        return fail(PBT_EINVAL, buf);
+    }
+    if (!a || !b || !c || !x || !g) return fail(PBT_EINVAL, "adjoint: null array pointer");
+    if (ds.flags & (PBT_FLAG_CYCLIC | PBT_FLAG_INPLACE))
+        return fail(PBT_EUNSUPPORTED, "adjoint: needs a non-cyclic plan without PBT_FLAG_INPLACE");
+    if (ds.precision == PBT_PREC_FP32_REFINE)
+        return fail(PBT_EUNSUPPORTED, "adjoint: provided for the fp64 and ff precisions");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    p->last_stream = s;
+    pbt::AdjointArgs adj;
+    adj.x = x;
+    adj.g = g;
+    adj.da = da;
+    adj.db = db;
+    adj.dc = dc;
+    const int arith = arith_of(ds.precision);
+    cudaError_t e;
+    if (p->thomas && ds.m <= 6) {
+        e = run_adjoint(arith, m, make_args(p, const_cast<double*>(a), const_cast<double*>(b),
+                                            const_cast<double*>(c), g, s, ds.nsys), adj);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+        return PBT_OK;
+    }
+    // Segmented plans, and m >= 7 (whose fused FP64 variant gives wrong
+    // results in the rolled-loop build: it is not used): materialise M^T and
+    // solve it with the plan's own forward method.
+    if (!p->at) {
+        const size_t n = (size_t)ds.m * ds.m * ds.nsys * ds.nrow;
+        if ((rc = alloc(p, &p->at, n)) || (rc = alloc(p, &p->bt, n)) || (rc = alloc(p, &p->ct, n))) return rc;
+    }
+    const pbt::SolveArgs g0 = make_args(p, const_cast<double*>(a), const_cast<double*>(b), const_cast<double*>(c),
+                                        g, s, ds.nsys);
+    if ((e = run_transpose_blocks(m, g0, p->at, p->bt, p->ct)) != cudaSuccess)
+        return cuda_fail(e, "adjoint: transpose launch");
+    if (p->thomas) {
+        e = run_thomas(arith, m, make_args(p, p->at, p->bt, p->ct, g, s, ds.nsys));
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint: transposed solve launch");
+    } else {
+        pbt::SolveArgs gs = make_args(p, p->at, p->bt, p->ct, g, s, ds.nsys * ds.nseg);
+        if ((e = run_modi(arith, m, gs)) != cudaSuccess ||
+            (e = run_reduced(arith, m, make_args(p, p->at, p->bt, p->ct, g, s, ds.nsys))) != cudaSuccess ||
+            (e = run_update(arith, m, gs)) != cudaSuccess)
+            return cuda_fail(e, "adjoint: transposed solve launch");
+    }
+    if ((e = run_gradients(m, g0, adj)) != cudaSuccess) return cuda_fail(e, "adjoint: gradient launch");
     return PBT_OK;
 }
 

@@ -18,7 +18,10 @@ template cudaError_t launch_modi<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_reduced<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_reduced_cyclic<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_update<PBT_NUM, PBT_M>(const SolveArgs&);
+template cudaError_t launch_adjoint<PBT_NUM, PBT_M>(const SolveArgs&, const AdjointArgs&);
 #ifdef PBT_NUM_IS_F64
+template cudaError_t launch_transpose_blocks<PBT_M>(const SolveArgs&, double*, double*, double*);
+template cudaError_t launch_gradients<PBT_M>(const SolveArgs&, const AdjointArgs&);
 template cudaError_t launch_residual<PBT_M>(const SolveArgs&, const double*, double*);
 template cudaError_t launch_accumulate<PBT_M>(const SolveArgs&, double*, const double*, unsigned*);
 #endif

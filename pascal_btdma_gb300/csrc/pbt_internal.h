@@ -46,6 +46,17 @@ template <class Num, int M> cudaError_t launch_modi(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced_cyclic(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_update(const SolveArgs& g);
+// Adjoint (pbt_kernels.cuh: k_adjoint, k_transpose_blocks, k_gradients).
+struct AdjointArgs {
+    const double* x;  // forward solution
+    double* g;        // in: dL/dx; out: lambda = dL/dd
+    double* da;       // gradient blocks (may be null)
+    double* db;
+    double* dc;
+};
+template <class Num, int M> cudaError_t launch_adjoint(const SolveArgs& g, const AdjointArgs& adj);
+template <int M> cudaError_t launch_transpose_blocks(const SolveArgs& g, double* At, double* Bt, double* Ct);
+template <int M> cudaError_t launch_gradients(const SolveArgs& g, const AdjointArgs& adj);
 // FP64 parts of the refined solve (instantiated with the F64 kernels).
 template <int M> cudaError_t launch_residual(const SolveArgs& g, const double* X, double* E);
 template <int M> cudaError_t launch_accumulate(const SolveArgs& g, double* X, const double* E, unsigned* stat);

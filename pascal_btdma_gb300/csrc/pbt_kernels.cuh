@@ -885,6 +885,212 @@ PBT_UNROLL
 }
 
 // ---------------------------------------------------------------------------
+// Adjoint.  For x = M^{-1} d and a loss L(x) with g = dL/dx, the gradients are
+// lambda = M^{-T} g = dL/dd and dL/dM = -lambda x^T on M's block pattern:
+//   dA_q = -lambda_q x_{q-1}^T,  dB_q = -lambda_q x_q^T,  dC_q = -lambda_q x_{q+1}^T
+// (dA_0 = dC_{N-1} = 0: those blocks never enter the non-cyclic solve).
+// M^T is block tridiagonal with the lower and upper blocks swapped and every
+// block transposed:  At_q = C_{q-1}^T,  Bt_q = B_q^T,  Ct_q = A_{q+1}^T.
+//
+// k_adjoint: single-segment block Thomas on M^T, reading A, B, C with
+// transposed indexing (no transposed copy), with the gradient assembly fused
+// into its backward sweep: when lambda_q is known, dB_q, dC_q and dA_{q+1} are
+// written.  The forward factors are recomputed (the forward solve's workspace
+// is reused for the adjoint's own C').  g holds dL/dx on entry and lambda on
+// return; da/db/dc may be null.
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_adjoint(const SolveArgs g, const AdjointArgs adj) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int N = g.nrow;
+    const size_t plane0 = (size_t)g.nsys * N;
+    const size_t rs = (size_t)g.nsys;
+    const double* A = g.a + sys;
+    const double* B = g.b + sys;
+    const double* C = g.c + sys;
+    double* G = adj.g + sys;
+    double* CW = g.cw + sys;
+    bool bad = false;
+
+    // Forward over the transposed rows.
+    T cp[M][M], y[M];
+    for (int q = 0; q < N; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        const bool last = (q == N - 1);
+        Acc r[M][M], x[M][M + 1];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            // row i of At_q = C_{q-1}^T: element (i, k) = C_{q-1}(k, i)
+            T ar[M];
+            if (q > 0) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) ar[k] = Num::in(C + o - rs + (size_t)(k + M * i) * plane);
+            }
+            Acc t = Num::acc(Num::in(G + o + (size_t)i * plane));
+            if (q > 0) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(t, ar[k], y[k]);
+            }
+            x[i][M] = t;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                Acc s = Num::acc(Num::in_ro(B + o + (size_t)(j + M * i) * plane));  // Bt_q(i, j) = B_q(j, i)
+                if (q > 0) {
+PBT_UNROLL
+                    for (int k = 0; k < M; ++k) Num::msub(s, ar[k], cp[k][j]);
+                }
+                r[i][j] = s;
+            }
+            if (PBT_ROW_FENCE) mem_fence_compiler();
+        }
+        if (!last) {
+            // Ct_q = A_{q+1}^T: element (i, j) = A_{q+1}(j, i)
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) x[i][j] = Num::acc(Num::in(A + o + rs + (size_t)(j + M * i) * plane));
+            gesv<Num, M, M + 1>(r, x, bad);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) cp[i][j] = Num::fin(x[i][j]);
+                y[i] = Num::fin(x[i][M]);
+            }
+            st_raw_blk<Num, M>(CW + o, plane, cp);
+            st_raw_vec<Num, M>(G + o, plane, y);
+        } else {
+            Acc xv[M][1];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) xv[i][0] = x[i][M];
+            gesv<Num, M, 1>(r, xv, bad);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) y[i] = Num::fin(xv[i][0]);
+        }
+    }
+    // Backward: lambda_q = y_q - Ct'_q lambda_{q+1}, with the gradient blocks.
+    const double* X = adj.x + sys;
+    double xq[M], xn[M];
+    T lam[M], lamn[M];
+    double lamd[M], lamnd[M];
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) {
+        lam[i] = y[i];
+        xq[i] = X[(size_t)(N - 1) * rs + (size_t)i * plane0];
+        lamn[i] = Num::zero();
+        lamnd[i] = 0.0;
+        xn[i] = 0.0;
+    }
+    for (int q = N - 1; q >= 0; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        if (q < N - 1) {
+            T c[M][M], t[M];
+            ld_raw_blk<Num, M>(c, CW + o, plane);
+            ld_raw_vec<Num, M>(t, G + o, plane);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                Acc s = Num::acc(t[i]);
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], lamn[k]);
+                lam[i] = Num::fin(s);
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) xq[i] = X[o + (size_t)i * plane];
+        }
+        out_vec<Num, M>(G + o, plane, lam);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) lamd[i] = G[o + (size_t)i * plane];
+        // dB_q = -lambda_q x_q^T; dC_q = -lambda_q x_{q+1}^T; dA_{q+1} = -lambda_{q+1} x_q^T
+        if (adj.db) {
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) adj.db[sys + o + (size_t)(i + M * j) * plane] = -lamd[i] * xq[j];
+        }
+        if (adj.dc) {
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i)
+                    adj.dc[sys + o + (size_t)(i + M * j) * plane] = (q < N - 1) ? -lamd[i] * xn[j] : 0.0;
+        }
+        if (adj.da) {
+            if (q < N - 1) {
+PBT_UNROLL
+                for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) adj.da[sys + o + rs + (size_t)(i + M * j) * plane] = -lamnd[i] * xq[j];
+            }
+            if (q == 0) {
+PBT_UNROLL
+                for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) adj.da[sys + (size_t)(i + M * j) * plane] = 0.0;
+            }
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            lamn[i] = lam[i];
+            lamnd[i] = lamd[i];
+            xn[i] = xq[i];
+        }
+    }
+    if (bad) atomicAdd(g.status, 1ull);
+}
+
+// Segmented adjoint, step 1: materialise M^T's blocks (At, Bt, Ct) in the
+// reference layout; step 3 (after the ordinary two-stage solve of M^T lambda
+// = g): the gradient blocks from lambda and x.  One thread per (system, row).
+template <int M>
+__global__ void k_transpose_blocks(const SolveArgs g, double* __restrict__ At, double* __restrict__ Bt,
+                                   double* __restrict__ Ct) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t plane = (size_t)g.nsys * g.nrow;
+    if (idx >= plane) return;
+    const int q = (int)(idx / (size_t)g.nsys);
+    const size_t rs = (size_t)g.nsys;
+PBT_UNROLL
+    for (int j = 0; j < M; ++j)
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            const size_t e = idx + (size_t)(i + M * j) * plane, et = (size_t)(j + M * i) * plane;
+            Bt[e] = __ldg(g.b + idx + et);
+            At[e] = (q > 0) ? __ldg(g.c + idx - rs + et) : 0.0;
+            Ct[e] = (q + 1 < g.nrow) ? __ldg(g.a + idx + rs + et) : 0.0;
+        }
+}
+
+template <int M>
+__global__ void k_gradients(const SolveArgs g, const AdjointArgs adj) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t plane = (size_t)g.nsys * g.nrow;
+    if (idx >= plane) return;
+    const int q = (int)(idx / (size_t)g.nsys);
+    const size_t rs = (size_t)g.nsys;
+    double lam[M], xm[M], x0[M], xp[M];
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) {
+        lam[i] = adj.g[idx + (size_t)i * plane];
+        x0[i] = __ldg(adj.x + idx + (size_t)i * plane);
+        xm[i] = (q > 0) ? __ldg(adj.x + idx - rs + (size_t)i * plane) : 0.0;
+        xp[i] = (q + 1 < g.nrow) ? __ldg(adj.x + idx + rs + (size_t)i * plane) : 0.0;
+    }
+PBT_UNROLL
+    for (int j = 0; j < M; ++j)
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            const size_t e = idx + (size_t)(i + M * j) * plane;
+            if (adj.da) adj.da[e] = -lam[i] * xm[j];
+            if (adj.db) adj.db[e] = -lam[i] * x0[j];
+            if (adj.dc) adj.dc[e] = -lam[i] * xp[j];
+        }
+}
+
+// ---------------------------------------------------------------------------
 // Iterative refinement (precision PBT_PREC_FP32_REFINE), FP64 parts.
 //   k_residual64: E = d - M X for every system, in FP64 (the one FP64 pass of
 //                 the refined solve): r_q = d_q - A_q x_{q-1} - B_q x_q - C_q x_{q+1}
@@ -985,6 +1191,24 @@ cudaError_t launch_reduced(const SolveArgs& g) {
 template <class Num, int M>
 cudaError_t launch_reduced_cyclic(const SolveArgs& g) {
     k_reduced_cyclic<Num, M><<<grid_x(g.nsys, g.tpb), g.tpb, 0, g.stream>>>(g);
+    return cudaGetLastError();
+}
+template <class Num, int M>
+cudaError_t launch_adjoint(const SolveArgs& g, const AdjointArgs& adj) {
+    const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
+    k_adjoint<Num, M><<<grid_x(g.nsys, tpb), tpb, 0, g.stream>>>(g, adj);
+    return cudaGetLastError();
+}
+template <int M>
+cudaError_t launch_transpose_blocks(const SolveArgs& g, double* At, double* Bt, double* Ct) {
+    const size_t n = (size_t)g.nsys * g.nrow;
+    k_transpose_blocks<M><<<(unsigned)((n + 255) / 256), 256, 0, g.stream>>>(g, At, Bt, Ct);
+    return cudaGetLastError();
+}
+template <int M>
+cudaError_t launch_gradients(const SolveArgs& g, const AdjointArgs& adj) {
+    const size_t n = (size_t)g.nsys * g.nrow;
+    k_gradients<M><<<(unsigned)((n + 255) / 256), 256, 0, g.stream>>>(g, adj);
     return cudaGetLastError();
 }
 template <int M>

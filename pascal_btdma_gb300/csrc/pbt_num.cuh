@@ -184,8 +184,8 @@ struct FF {
 
 // ---------------------------------------------------------------------------
 // F32: plain IEEE float, for the FP32 factorisation of the refined solve.
-// Inputs are rounded to float on load; raw workspace slots (8 bytes) hold the
-// float in their first 4 bytes.
+// Inputs are truncated to float on load; raw workspace slots (8 bytes) hold
+// the float in their first 4 bytes.
 struct F32 {
     using T = float;
     struct Acc {
@@ -193,11 +193,16 @@ struct F32 {
     };
     static constexpr bool kConv = true;
 
-    __device__ static __forceinline__ T in(const double* p) { return __double2float_rn(*p); }
-    __device__ static __forceinline__ T in_ro(const double* p) { return __double2float_rn(__ldg(p)); }
-    __device__ static __forceinline__ void out(double* p, T v) { *p = static_cast<double>(v); }
-    __device__ static __forceinline__ T lds(const double* p) { return *reinterpret_cast<const float*>(p); }
-    __device__ static __forceinline__ void sts(double* p, T v) { *reinterpret_cast<float*>(p) = v; }
+    // Conversions by bit manipulation (FF::split's high part truncates to 24
+    // bits; FF::widen is exact): GB300 runs F2F conversions with a double
+    // operand at the FP64 rate, which would cost more than the solve itself.
+    __device__ static __forceinline__ T in(const double* p) { return FF::split(*p).h; }
+    __device__ static __forceinline__ T in_ro(const double* p) { return FF::split(__ldg(p)).h; }
+    __device__ static __forceinline__ void out(double* p, T v) { *p = FF::widen(v); }
+    // Raw slots are written whole (the float and a zero pad), so every 32-byte
+    // sector of a warp's store is complete and L2 never has to fetch the rest.
+    __device__ static __forceinline__ T lds(const double* p) { return reinterpret_cast<const float2*>(p)->x; }
+    __device__ static __forceinline__ void sts(double* p, T v) { *reinterpret_cast<float2*>(p) = make_float2(v, 0.f); }
 
     __device__ static __forceinline__ Acc acc(T x) { return {x}; }
     __device__ static __forceinline__ Acc acc0() { return {0.f}; }
