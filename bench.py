@@ -55,6 +55,10 @@ VARIANTS = [  # name, m, nsys, nrow, nseg, delta
 # log-uniform factor in [1e-3, 1e3]; FP32 factorisation + FP64 residual
 # refinement, and float-float, each against the plain FP64 solution.
 MIXED = [(1.05, 1), (1.05, 16), (1.5, 1), (1.5, 16)]  # (delta, nseg)
+# Adjoint: m=4, nsys=16384, N=512, delta=1.5, forward and adjoint at P=8 and
+# P=1; memory-pressure variant: nsys=262144 (the 16384-system batch tiled 16x
+# on the device), factors recomputed by the adjoint.
+ADJ = dict(m=4, nsys=16384, nrow=512, delta=1.5, segs=(8, 1), pressure_tiles=16)
 
 
 def bytes_per_row(m: int, width: int = 8) -> int:
@@ -397,6 +401,59 @@ def run_ours(args):
         del ma, mb, mc, md, mw
         torch.cuda.empty_cache()
 
+    adjoint = {}
+    aw, _ = make_workload(ADJ["m"], ADJ["nsys"], ADJ["nrow"], ADJ["delta"], dev)
+    am, an, anr = ADJ["m"], ADJ["nsys"], ADJ["nrow"]
+    A0, B0, C0, D0 = (torch.from_numpy(x).to(dev) for x in aw.arrays)
+
+    def time_adjoint(plan, A_, B_, C_, D_, m_, ns_, nr_, k):
+        x_ = D_.clone()
+        solve(plan, A_, B_, C_, x_, m_, ns_, nr_)
+        gsrc = torch.ones_like(D_)
+        da_, db_, dc_ = torch.empty_like(A_), torch.empty_like(B_), torch.empty_like(C_)
+        lam_ = gsrc.clone()
+        for _ in range(2):
+            lam_.copy_(gsrc)
+            pbt.adjoint_noncyclic(plan, A_, B_, C_, x_, lam_, da_, db_, dc_)
+        torch.cuda.synchronize()
+        bufs = [gsrc.clone() for _ in range(k)]
+        st_ = torch.cuda.current_stream()
+        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0_.record(st_)
+        for i_ in range(k):
+            pbt.adjoint_noncyclic(plan, A_, B_, C_, x_, bufs[i_], da_, db_, dc_)
+        e1_.record(st_)
+        torch.cuda.synchronize()
+        return e0_.elapsed_time(e1_) / 1e3 / k
+
+    for nseg_a in ADJ["segs"]:
+        for prec in ("ff", "fp64"):
+            with pbt.BtdmaGpuPlan() as pl:
+                pl.create(am, an, anr, nseg_a, precision=prec)
+                fs = time_device(pl, (A0, B0, C0), [D0], am, an, anr, 3, 3, ws, dev, solve) / 3
+                ad = time_adjoint(pl, A0, B0, C0, D0, am, an, anr, 3)
+            adjoint[f"{prec}_P{nseg_a}"] = {"forward_ms": fs * 1e3, "adjoint_ms": ad * 1e3,
+                                            "adjoint_over_forward": ad / fs,
+                                            "fused": nseg_a == 1 and am <= 6}
+    # memory pressure: 262144 systems, adjoint recomputes the factorisation
+    tiles = ADJ["pressure_tiles"]
+    ns_p = an * tiles
+
+    def tile(t, w_):
+        return t.view(-1, an).repeat(1, tiles).contiguous().view(-1)
+
+    Ap, Bp, Cp, Dp = (tile(t, aw) for t in (A0, B0, C0, D0))
+    del A0, B0, C0, D0
+    with pbt.BtdmaGpuPlan() as pl:
+        pl.create(am, ns_p, anr, 1, precision="ff")
+        fs = time_device(pl, (Ap, Bp, Cp), [Dp], am, ns_p, anr, 2, 3, ws, dev, solve) / 2
+        ad = time_adjoint(pl, Ap, Bp, Cp, Dp, am, ns_p, anr, 2)
+    adjoint["ff_P1_nsys262144"] = {"forward_ms": fs * 1e3, "adjoint_ms": ad * 1e3,
+                                   "adjoint_over_forward": ad / fs, "fused": True,
+                                   "device_bytes_inputs": 8 * (3 * am * am + am) * ns_p * anr}
+    del Ap, Bp, Cp, Dp, aw
+    torch.cuda.empty_cache()
+
     result = {
         "metric": "block-rows/s (chosen method at <=1e-10 rel err vs plain FP64)",
         "value": value,
@@ -432,6 +489,7 @@ def run_ours(args):
         "clocks": clocks,
         "variants": variants,
         "mixed_precision": mixed,
+        "adjoint": adjoint,
     }
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(m, nrow, nseg, DELTA, target_s=args.cpu_seconds)
