@@ -59,6 +59,86 @@ MIXED = [(1.05, 1), (1.05, 16), (1.5, 1), (1.5, 16)]  # (delta, nseg)
 # P=1; memory-pressure variant: nsys=262144 (the 16384-system batch tiled 16x
 # on the device), factors recomputed by the adjoint.
 ADJ = dict(m=4, nsys=16384, nrow=512, delta=1.5, segs=(8, 1), pressure_tiles=16)
+# Uneven batch: 32768 systems, N log-uniform in [16, 4096], m uniform in
+# {2, 3, 4, 5}, delta = 1.5; one persistent launch per sweep, 100 sweeps in a
+# CUDA graph; tuning by the autotuner; against one plain launch per (m, N).
+UNEVEN = dict(nsys=32768, nmin=16, nmax=4096, mmin=2, mmax=5, delta=1.5, sweeps=100)
+
+
+def run_uneven(dev, log=None) -> dict:
+    import torch
+
+    import pascal_btdma_gb300 as pbt
+    from pascal_btdma_gb300 import batch as B
+    from pascal_btdma_gb300 import synth
+
+    u = UNEVEN
+    n, m = synth.uneven_shapes(SEED, u["nsys"], u["nmin"], u["nmax"], u["mmin"], u["mmax"])
+    A, Bm, Cm, D, mo, vo = synth.fill_batch(m, n, seed=SEED, delta=u["delta"])
+    user = tuple(torch.from_numpy(x).to(dev) for x in (A, Bm, Cm, D))
+    rows = int(n.sum())
+    out = {"nsys": u["nsys"], "block_rows": rows, "distinct_m_n": int(len(set(zip(m.tolist(), n.tolist()))))}
+    for prec in ("fp64", "ff"):
+        tuning = B.autotune(m, n, user, prec, log=log)
+        plan = B.BatchPlan(m, n, prec, tuning)
+        packed = plan.pack(*user)
+        d0 = packed[3].clone()
+        g = B.capture_sweeps(plan, packed, d0, sweeps=u["sweeps"])
+        g.replay()  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        plan.status()
+        t = e0.elapsed_time(e1) / 1e3 / u["sweeps"]
+        out[prec] = {"block_rows_per_s": rows / t, "ms_per_sweep": t * 1e3, "tuning": tuning, **plan.info()}
+        plan.destroy()
+        del packed, d0, g
+    # Plain launches: one uniform plan and one solve per distinct (m, N).
+    groups = {}
+    for s in range(u["nsys"]):
+        groups.setdefault((int(m[s]), int(n[s])), []).append(s)
+    plans, arrays = [], []
+    for (mm, nn), idx in groups.items():
+        k = len(idx)
+        def gather(src, off, per):
+            cols = [src[int(off[s]):int(off[s]) + per] for s in idx]
+            return torch.stack(cols, dim=1).reshape(-1).contiguous()   # (e, row) x sys -> reference layout
+        a_ = gather(user[0], mo, nn * mm * mm)
+        b_ = gather(user[1], mo, nn * mm * mm)
+        c_ = gather(user[2], mo, nn * mm * mm)
+        d_ = gather(user[3], vo, nn * mm)
+        plans.append(pbt.BtdmaGpuPlan().create(mm, k, nn, 1, precision="fp64"))
+        arrays.append((a_, b_, c_, d_, d_.clone(), mm, k, nn))
+    torch.cuda.synchronize()
+
+    # One launch per (m, N) group, spread round-robin over 32 streams so the
+    # many small, latency-bound solves overlap (one stream serialises them
+    # into minutes per sweep).
+    streams = [torch.cuda.Stream() for _ in range(32)]
+
+    def sweep():
+        for i, (pl, (a_, b_, c_, d_, w_, mm, k, nn)) in enumerate(zip(plans, arrays)):
+            st = streams[i % len(streams)]
+            with torch.cuda.stream(st):
+                w_.copy_(d_)
+                pbt.solve_noncyclic(pl, a_, b_, c_, w_, mm, k, nn, stream=st)
+
+    sweep()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sweep()
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    out["plain_per_m_n_fp64"] = {"block_rows_per_s": rows / t, "ms_per_sweep": t * 1e3, "launches": len(plans),
+                                 "streams": len(streams), "timing": "host wall clock, one sweep after one warm-up"}
+    for pl in plans:
+        pl.destroy()
+    del arrays, user
+    torch.cuda.empty_cache()
+    return out
 
 
 def bytes_per_row(m: int, width: int = 8) -> int:
@@ -453,6 +533,7 @@ def run_ours(args):
                                    "device_bytes_inputs": 8 * (3 * am * am + am) * ns_p * anr}
     del Ap, Bp, Cp, Dp, aw
     torch.cuda.empty_cache()
+    uneven = run_uneven(dev)
 
     result = {
         "metric": "block-rows/s (chosen method at <=1e-10 rel err vs plain FP64)",
@@ -490,6 +571,7 @@ def run_ours(args):
         "variants": variants,
         "mixed_precision": mixed,
         "adjoint": adjoint,
+        "uneven_batch": uneven,
     }
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(m, nrow, nseg, DELTA, target_s=args.cpu_seconds)

@@ -49,6 +49,16 @@ double pbt_synth_uniform(uint64_t seed, uint32_t stream, uint32_t sys, uint32_t 
 int pbt_synth_fill(int kind, unsigned flags, int m, int nsys, int N, uint64_t seed, double delta,
                    double* A, double* B, double* C, double* D, double* x_ref, int nthreads);
 
+/* An uneven batch in the per-system layout of include/pbt_batch.h: system s
+ * (block size m[s], length nrow[s]) at matrix offset mat_off[s] and vector
+ * offset vec_off[s], each in the reference layout of a single system.  The
+ * values of system s are those pbt_synth_fill gives system index s of a
+ * uniform batch with the same m and nrow (counter sys = s), for the
+ * DOMINANT and DIAGONAL kinds.  Threads split the systems. */
+int pbt_synth_fill_batch(int kind, unsigned flags, int nsys, const int* m, const int* nrow,
+                         const long long* mat_off, const long long* vec_off, uint64_t seed, double delta,
+                         double* A, double* B, double* C, double* D, int nthreads);
+
 /* Per-system shapes of the uneven batch: N log-uniform integer in
  * [nmin, nmax], m uniform in [mmin, mmax]; stream 5 of the seed. */
 int pbt_synth_uneven_shapes(uint64_t seed, int nsys, int nmin, int nmax, int mmin, int mmax,

@@ -102,6 +102,10 @@ SYNTH_SIGNATURES = {
         [C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P],
     ),
     "pbt_synth_exp2": (C.c_double, [C.c_double]),
+    "pbt_synth_fill_batch": (
+        C.c_int,
+        [C.c_int, C.c_uint, C.c_int, _P, _P, _P, _P, C.c_uint64, C.c_double, _P, _P, _P, _P, C.c_int],
+    ),
 }
 
 _lib = None

@@ -34,7 +34,8 @@ MAX_BLOCK = 10
 
 # Families of kernels instantiated per block size: (source, object stem).
 PER_M_SOURCES = [("pbt_inst.cu", "F64"), ("pbt_inst.cu", "FF"), ("pbt_inst.cu", "F32")]
-HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu", "pbt_noalloc.cu"]
+HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu", "pbt_noalloc.cu", "pbt_batch.cpp", "pbt_batch_f64.cu",
+                "pbt_batch_ff.cu"]
 
 
 def _nvcc() -> str:
@@ -79,7 +80,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     for src in HOST_SOURCES:
         obj = BUILD / (Path(src).stem + ".o")
         objs.append(obj)
-        if _stale(obj, [CSRC / src] + hdrs + sorted(INCLUDE.glob("*.h"))):
+        if _stale(obj, [CSRC / src] + hdrs + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))):
             tasks.append((obj, [nvcc, *NVCC_FLAGS, "-x", "cu", "-c", str(CSRC / src), "-o", str(obj)]))
     jobs = jobs or max(2, os.cpu_count() or 2)
     if tasks:

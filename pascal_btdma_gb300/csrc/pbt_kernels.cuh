@@ -203,50 +203,6 @@ __device__ __forceinline__ void ld_fac_blk(typename Num::T (&x)[M][M], const dou
         in_blk<Num, M>(x, base, plane);
 }
 
-// L2 prefetch of one block row of A, B, C and D for the warp's 32 systems:
-// the 3*M*M + M element planes of the row, each a run of up to 32 doubles
-// that spans at most three 128-byte lines, spread over the lanes (about
-// (3*M*M + M) * 3 / 32 prefetch instructions per lane).  Addresses are
-// clamped to the last system, so a partial warp never names memory outside
-// the arrays.
-template <int M>
-__device__ __forceinline__ void prefetch_row(const double* A, const double* B, const double* C, const double* D,
-                                             int warp_sys0, int nsys, size_t row_off, size_t plane) {
-    constexpr int kPlanes = 3 * M * M + M;
-    const int lane = threadIdx.x & 31;
-#pragma unroll 1
-    for (int idx = lane; idx < 3 * kPlanes; idx += 32) {
-        const int pl = idx / 3, part = idx - 3 * pl;
-        int s = warp_sys0 + (part == 0 ? 0 : (part == 1 ? 16 : 31));
-        s = s < nsys ? s : nsys - 1;
-        const double* base;
-        int e;
-        if (pl < M * M) { base = A; e = pl; }
-        else if (pl < 2 * M * M) { base = B; e = pl - M * M; }
-        else if (pl < 3 * M * M) { base = C; e = pl - 2 * M * M; }
-        else { base = D; e = pl - 3 * M * M; }
-        const double* addr = base + (size_t)s + row_off + (size_t)e * plane;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
-    }
-}
-
-// L2 prefetch of the workspace row (C' and y) read by the backward sweep.
-template <int M>
-__device__ __forceinline__ void prefetch_back_row(const double* CW, const double* D, int warp_sys0, int nsys,
-                                                  size_t row_off, size_t plane) {
-    constexpr int kPlanes = M * M + M;
-    const int lane = threadIdx.x & 31;
-#pragma unroll 1
-    for (int idx = lane; idx < 3 * kPlanes; idx += 32) {
-        const int pl = idx / 3, part = idx - 3 * pl;
-        int s = warp_sys0 + (part == 0 ? 0 : (part == 1 ? 16 : 31));
-        s = s < nsys ? s : nsys - 1;
-        const double* addr = (pl < M * M ? CW + (size_t)pl * plane : D + (size_t)(pl - M * M) * plane) +
-                             (size_t)s + row_off;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
-    }
-}
-
 template <class Num, int M>
 __device__ __forceinline__ void to_acc(typename Num::Acc (&d)[M][M], const typename Num::T (&s)[M][M]) {
 PBT_UNROLL
@@ -273,11 +229,6 @@ PBT_UNROLL
 #ifndef PBT_THOMAS_MAXNREG
 #define PBT_THOMAS_MAXNREG 128
 #endif
-// Rows of A, B, C, D prefetched into L2 ahead of the row being eliminated
-// (measured no gain on GB300: off).
-#ifndef PBT_PREFETCH_ROWS
-#define PBT_PREFETCH_ROWS 0
-#endif
 // Compiler fence between the block rows of one row's loads (keeps only one
 // row of A and B live; 0 lets the compiler hoist all of a row's loads).
 #ifndef PBT_ROW_FENCE
@@ -285,33 +236,19 @@ PBT_UNROLL
 #endif
 constexpr int kThomasThreads = PBT_THOMAS_THREADS;
 
+// Geometry of one solve as a body sees it: pointers already offset to the
+// thread's system (and segment), `plane` = element-plane stride, `rs` = row
+// stride (the number of systems interleaved in the layout).
 template <class Num, int M>
-__global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
+__device__ __forceinline__ void thomas_body(const double* A, const double* B, const double* C, double* D,
+                                            double* CW, size_t plane0, size_t rs, int N, bool raw, bool& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
-    const int warp_sys0 = sys & ~31;
-    const int N = g.nrow;
-    const size_t plane0 = (size_t)g.nsys * N;
-    const size_t rs = (size_t)g.nsys;
-    const double* A = g.a + sys;
-    const double* B = g.b + sys;
-    const double* C = g.c + sys;
-    double* D = g.d + sys;
-    double* CW = g.cw + sys;
-    const bool raw = g.factors_raw != 0;
-    bool bad = false;
-
     T cp[M][M], y[M];
-    for (int q = 0; q < PBT_PREFETCH_ROWS && q < N; ++q)
-        prefetch_row<M>(g.a, g.b, g.c, g.d, warp_sys0, g.nsys, (size_t)q * rs, plane0);
     for (int q = 0; q < N; ++q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         const bool last = (q == N - 1);
-        if (PBT_PREFETCH_ROWS > 0 && q + PBT_PREFETCH_ROWS < N)
-            prefetch_row<M>(g.a, g.b, g.c, g.d, warp_sys0, g.nsys, o + PBT_PREFETCH_ROWS * rs, plane);
         Acc r[M][M], x[M][M + 1];
 PBT_UNROLL
         for (int i = 0; i < M; ++i) {
@@ -364,7 +301,6 @@ PBT_UNROLL
     for (int q = N - 2; q >= 0; --q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
-        if (q > 0) prefetch_back_row<M>(g.cw, g.d, warp_sys0, g.nsys, o - rs, plane);
         T c[M][M], t[M];
         ld_fac_blk<Num, M>(c, CW + o, plane, raw);
         ld_raw_vec<Num, M>(t, D + o, plane);
@@ -379,35 +315,29 @@ PBT_UNROLL
         for (int i = 0; i < M; ++i) y[i] = t[i];
         out_vec<Num, M>(D + o, plane, y);
     }
+}
+
+template <class Num, int M>
+__global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    bool bad = false;
+    thomas_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
+                        (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
     if (bad) atomicAdd(g.status, 1ull);
 }
 
 // ---------------------------------------------------------------------------
 // Stage 1: modified elimination of one segment (rows f..l, n = l - f + 1).
 // ---------------------------------------------------------------------------
+// A..CW point at the segment's first row of this system; RA..RD at this
+// system in the reduced layout (row stride rrs, plane stride rplane).
 template <class Num, int M>
-__global__ void __launch_bounds__(128) k_modi(const SolveArgs g) {
+__device__ __forceinline__ void modi_body(const double* A, const double* B, const double* C, double* D, double* AW,
+                                          double* CW, size_t plane0, size_t rs, int n, bool raw, double* RA,
+                                          double* RC, double* RD, size_t rplane, size_t rrs, int seg, bool& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
-    const int seg = blockIdx.y;
-    int f, l;
-    seg_rows(g.nrow, g.nseg, seg, f, l);
-    const int n = l - f + 1;
-    const size_t plane0 = (size_t)g.nsys * g.nrow;
-    const size_t rs = (size_t)g.nsys;
-    const size_t fo = (size_t)f * rs + sys;
-    const double* A = g.a + fo;
-    const double* B = g.b + fo;
-    const double* C = g.c + fo;
-    double* D = g.d + fo;
-    double* AW = g.aw + fo;
-    double* CW = g.cw + fo;
-    const bool raw = g.factors_raw != 0;
-    const int R = 2 * g.nseg;
-    const size_t rplane = (size_t)g.nsys * R;
-    bool bad = false;
 
     T ap[M][M], cp[M][M], dp[M];
     // Rows 1 and 2 of the segment: [A'|C'|d'] = B^{-1}[A|C|d]; rows 3..n:
@@ -466,10 +396,10 @@ PBT_UNROLL
     }
     // Reduced row 2*seg+1 = the segment's last row (A'_n, C'_n, d'_n).
     {
-        const size_t ro = (size_t)sys + rs * (size_t)(2 * seg + 1);
-        st_raw_blk<Num, M>(g.ra + ro, rplane, ap);
-        st_raw_blk<Num, M>(g.rc + ro, rplane, cp);
-        st_raw_vec<Num, M>(g.rd + ro, rplane, dp);
+        const size_t ro = rrs * (size_t)(2 * seg + 1);
+        st_raw_blk<Num, M>(RA + ro, rplane, ap);
+        st_raw_blk<Num, M>(RC + ro, rplane, cp);
+        st_raw_vec<Num, M>(RD + ro, rplane, dp);
     }
     // Backward sweep, rows n-2 .. 2 (1-based): carried row = q+1.
     {
@@ -574,11 +504,25 @@ PBT_UNROLL
         st_fac_blk<Num, M>(AW, plane, ap, raw);
         st_fac_blk<Num, M>(CW, plane, cp, raw);
         st_raw_vec<Num, M>(D, plane, dp);
-        const size_t ro = (size_t)sys + rs * (size_t)(2 * seg);
-        st_raw_blk<Num, M>(g.ra + ro, rplane, ap);
-        st_raw_blk<Num, M>(g.rc + ro, rplane, cp);
-        st_raw_vec<Num, M>(g.rd + ro, rplane, dp);
+        const size_t ro = rrs * (size_t)(2 * seg);
+        st_raw_blk<Num, M>(RA + ro, rplane, ap);
+        st_raw_blk<Num, M>(RC + ro, rplane, cp);
+        st_raw_vec<Num, M>(RD + ro, rplane, dp);
     }
+}
+
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_modi(const SolveArgs g) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int seg = blockIdx.y;
+    int f, l;
+    seg_rows(g.nrow, g.nseg, seg, f, l);
+    const size_t rs = (size_t)g.nsys;
+    const size_t fo = (size_t)f * rs + sys;
+    bool bad = false;
+    modi_body<Num, M>(g.a + fo, g.b + fo, g.c + fo, g.d + fo, g.aw + fo, g.cw + fo, rs * g.nrow, rs, l - f + 1,
+                      g.factors_raw != 0, g.ra + sys, g.rc + sys, g.rd + sys, rs * 2 * g.nseg, rs, seg, bad);
     if (bad) atomicAdd(g.status, 1ull);
 }
 
@@ -587,18 +531,10 @@ PBT_UNROLL
 // row R-1's C are never read.  C' overwrites rc, the solution overwrites rd.
 // ---------------------------------------------------------------------------
 template <class Num, int M>
-__global__ void __launch_bounds__(128) k_reduced(const SolveArgs g) {
+__device__ __forceinline__ void reduced_body(const double* RA, double* RC, double* RD, size_t plane0, size_t rs,
+                                             int R, bool& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
-    const int R = 2 * g.nseg;
-    const size_t plane0 = (size_t)g.nsys * R;
-    const size_t rs = (size_t)g.nsys;
-    const double* RA = g.ra + sys;
-    double* RC = g.rc + sys;
-    double* RD = g.rd + sys;
-    bool bad = false;
 
     T cp[M][M], y[M];
     // Row 0: B = I, so [C'|y] = [C|d] exactly.
@@ -667,6 +603,15 @@ PBT_UNROLL
         for (int i = 0; i < M; ++i) y[i] = t[i];
         st_raw_vec<Num, M>(RD + o, plane, y);
     }
+}
+
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_reduced(const SolveArgs g) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    bool bad = false;
+    const size_t rs = (size_t)g.nsys;
+    reduced_body<Num, M>(g.ra + sys, g.rc + sys, g.rd + sys, rs * 2 * g.nseg, rs, 2 * g.nseg, bad);
     if (bad) atomicAdd(g.status, 1ull);
 }
 
@@ -841,27 +786,13 @@ PBT_UNROLL
 // Stage 3: interior update of one segment from the reduced solution.
 // ---------------------------------------------------------------------------
 template <class Num, int M>
-__global__ void __launch_bounds__(128) k_update(const SolveArgs g) {
+__device__ __forceinline__ void update_body(const double* AW, const double* CW, double* D, size_t plane0, size_t rs,
+                                            int n, bool raw, const double* RD, size_t rplane, size_t rrs, int seg) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
-    const int seg = blockIdx.y;
-    int f, l;
-    seg_rows(g.nrow, g.nseg, seg, f, l);
-    const int n = l - f + 1;
-    const size_t plane0 = (size_t)g.nsys * g.nrow;
-    const size_t rs = (size_t)g.nsys;
-    const size_t fo = (size_t)f * rs + sys;
-    const double* AW = g.aw + fo;
-    const double* CW = g.cw + fo;
-    double* D = g.d + fo;
-    const bool raw = g.factors_raw != 0;
-    const int R = 2 * g.nseg;
-    const size_t rplane = (size_t)g.nsys * R;
     T x0[M], xn[M];
-    ld_raw_vec<Num, M>(x0, g.rd + sys + rs * (size_t)(2 * seg), rplane);
-    ld_raw_vec<Num, M>(xn, g.rd + sys + rs * (size_t)(2 * seg + 1), rplane);
+    ld_raw_vec<Num, M>(x0, RD + rrs * (size_t)(2 * seg), rplane);
+    ld_raw_vec<Num, M>(xn, RD + rrs * (size_t)(2 * seg + 1), rplane);
     out_vec<Num, M>(D, plane0, x0);
     out_vec<Num, M>(D + (size_t)(n - 1) * rs, plane0, xn);
     for (int q = 1; q < n - 1; ++q) {
@@ -882,6 +813,19 @@ PBT_UNROLL
         }
         out_vec<Num, M>(D + o, plane, t);
     }
+}
+
+template <class Num, int M>
+__global__ void __launch_bounds__(128) k_update(const SolveArgs g) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    const int seg = blockIdx.y;
+    int f, l;
+    seg_rows(g.nrow, g.nseg, seg, f, l);
+    const size_t rs = (size_t)g.nsys;
+    const size_t fo = (size_t)f * rs + sys;
+    update_body<Num, M>(g.aw + fo, g.cw + fo, g.d + fo, rs * g.nrow, rs, l - f + 1, g.factors_raw != 0, g.rd + sys,
+                        rs * 2 * g.nseg, rs, seg);
 }
 
 // ---------------------------------------------------------------------------

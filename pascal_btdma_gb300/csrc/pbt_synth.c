@@ -228,6 +228,104 @@ int pbt_synth_fill(int kind, unsigned flags, int m, int nsys, int N, uint64_t se
     return 0;
 }
 
+typedef struct {
+    int kind;
+    unsigned flags;
+    int nsys;
+    const int* m;
+    const int* nrow;
+    const long long* mat_off;
+    const long long* vec_off;
+    uint64_t seed;
+    double delta;
+    double *A, *B, *C, *D;
+    int s0, s1;
+} batch_job;
+
+/* One system s of a batch: the DOMINANT / DIAGONAL formulas of fill_chunk
+ * with nsys = 1 storage at the system's own offsets and counter sys = s. */
+static void* fill_batch_chunk(void* arg) {
+    const batch_job* jb = (const batch_job*)arg;
+    for (int s = jb->s0; s < jb->s1; ++s) {
+        const int m = jb->m[s], N = jb->nrow[s];
+        double* A = jb->A + jb->mat_off[s];
+        double* B = jb->B + jb->mat_off[s];
+        double* C = jb->C + jb->mat_off[s];
+        double* D = jb->D + jb->vec_off[s];
+        const int zero_ends = (jb->flags & PBT_SYNTH_ZERO_ENDS) != 0;
+#define BM(row, i, j) ((size_t)(row) + (size_t)N * ((size_t)(i) + (size_t)m * (size_t)(j)))
+#define BV(row, i) ((size_t)(row) + (size_t)N * (size_t)(i))
+        for (int row = 0; row < N; ++row) {
+            if (jb->kind == PBT_SYNTH_DIAGONAL) {
+                for (int j = 0; j < m; ++j) {
+                    for (int i = 0; i < m; ++i) {
+                        A[BM(row, i, j)] = (i == j) ? 0.25 : 0.0;
+                        B[BM(row, i, j)] = (i == j) ? 2.0 : 0.0;
+                        C[BM(row, i, j)] = (i == j) ? 0.25 : 0.0;
+                    }
+                    D[BV(row, j)] = 1.0;
+                }
+                continue;
+            }
+            const int a_zero = zero_ends && row == 0;
+            const int c_zero = zero_ends && row == N - 1;
+            for (int j = 0; j < m; ++j)
+                for (int i = 0; i < m; ++i) {
+                    const int e = i + m * j;
+                    A[BM(row, i, j)] = a_zero ? 0.0 : pbt_synth_uniform(jb->seed, 0, (uint32_t)s, row, e);
+                    B[BM(row, i, j)] = pbt_synth_uniform(jb->seed, 1, (uint32_t)s, row, e);
+                    C[BM(row, i, j)] = c_zero ? 0.0 : pbt_synth_uniform(jb->seed, 2, (uint32_t)s, row, e);
+                }
+            for (int i = 0; i < m; ++i) {
+                double t = 0.0;
+                for (int j = 0; j < m; ++j) t = t + fabs(A[BM(row, i, j)]);
+                for (int j = 0; j < m; ++j) t = t + fabs(C[BM(row, i, j)]);
+                for (int j = 0; j < m; ++j) t = t + fabs(B[BM(row, i, j)]);
+                B[BM(row, i, i)] = B[BM(row, i, i)] + jb->delta * t;
+                D[BV(row, i)] = pbt_synth_uniform(jb->seed, 3, (uint32_t)s, row, (uint32_t)i);
+            }
+        }
+#undef BM
+#undef BV
+    }
+    return NULL;
+}
+
+int pbt_synth_fill_batch(int kind, unsigned flags, int nsys, const int* m, const int* nrow, const long long* mat_off,
+                         const long long* vec_off, uint64_t seed, double delta, double* A, double* B, double* C,
+                         double* D, int nthreads) {
+    if (nsys < 1 || !m || !nrow || !mat_off || !vec_off || !A || !B || !C || !D) return -1;
+    if (kind != PBT_SYNTH_DOMINANT && kind != PBT_SYNTH_DIAGONAL) return -1;
+    for (int s = 0; s < nsys; ++s)
+        if (m[s] < 1 || m[s] > 16 || nrow[s] < 1) return -1;
+    if (nthreads <= 0) {
+        long n = sysconf(_SC_NPROCESSORS_ONLN);
+        nthreads = n > 0 ? (int)n : 1;
+    }
+    if (nthreads > nsys) nthreads = nsys;
+    batch_job* jobs = (batch_job*)calloc((size_t)nthreads, sizeof(batch_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!jobs || !th) {
+        free(jobs);
+        free(th);
+        return -1;
+    }
+    for (int t = 0; t < nthreads; ++t) {
+        /* interleaved chunks balance long and short systems */
+        const int base = nsys / nthreads, rem = nsys % nthreads;
+        const int f = t * base + (t < rem ? t : rem);
+        const int n = base + (t < rem ? 1 : 0);
+        batch_job j = {kind, flags, nsys, m, nrow, mat_off, vec_off, seed, delta, A, B, C, D, f, f + n};
+        jobs[t] = j;
+    }
+    for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, fill_batch_chunk, &jobs[t]);
+    fill_batch_chunk(&jobs[0]);
+    for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(jobs);
+    free(th);
+    return 0;
+}
+
 int pbt_synth_uneven_shapes(uint64_t seed, int nsys, int nmin, int nmax, int mmin, int mmax, int* n_out,
                             int* m_out) {
     if (nsys < 1 || nmin < 1 || nmax < nmin || mmin < 1 || mmax < mmin || !n_out || !m_out) return -1;

@@ -100,3 +100,22 @@ def uneven_shapes(seed: int, nsys: int, nmin=16, nmax=4096, mmin=2, mmax=5) -> t
     if rc != 0:
         raise ValueError("pbt_synth_uneven_shapes rejected its arguments")
     return n, m
+
+
+def fill_batch(m_per_sys, n_per_sys, seed=0, delta=1.5, kind=DOMINANT, flags=ZERO_ENDS, nthreads=0, alloc=None):
+    """An uneven batch in the per-system layout of include/pbt_batch.h.
+    Returns (A, B, C, D, mat_off, vec_off) as flat numpy arrays."""
+    m = np.ascontiguousarray(m_per_sys, dtype=np.int32)
+    n = np.ascontiguousarray(n_per_sys, dtype=np.int32)
+    mo = np.concatenate([[0], np.cumsum(n.astype(np.int64) * m * m)[:-1]]).astype(np.int64)
+    vo = np.concatenate([[0], np.cumsum(n.astype(np.int64) * m)[:-1]]).astype(np.int64)
+    nm = int((n.astype(np.int64) * m * m).sum())
+    nv = int((n.astype(np.int64) * m).sum())
+    mk = alloc or (lambda k: np.empty(k, dtype=np.float64))
+    A, B, Cc, D = mk(nm), mk(nm), mk(nm), mk(nv)
+    rc = N.synth_lib().pbt_synth_fill_batch(int(kind), int(flags), int(m.size), m.ctypes.data, n.ctypes.data,
+                                            mo.ctypes.data, vo.ctypes.data, C.c_uint64(seed), float(delta),
+                                            _p(A), _p(B), _p(Cc), _p(D), int(nthreads))
+    if rc != 0:
+        raise ValueError("pbt_synth_fill_batch rejected its arguments")
+    return A, B, Cc, D, mo, vo

@@ -20,7 +20,8 @@ def declared(header: str) -> set[str]:
     return set(re.findall(r"\b(pbt_[a-z0-9_]+)\s*\(", text))
 
 
-@pytest.mark.parametrize("header,loader", [("pbt.h", N.lib), ("pbt_probe.h", N.lib), ("pbt_synth.h", N.synth_lib)])
+@pytest.mark.parametrize("header,loader", [("pbt.h", N.lib), ("pbt_probe.h", N.lib), ("pbt_batch.h", N.lib),
+                                           ("pbt_synth.h", N.synth_lib)])
 def test_every_declared_symbol_is_exported(header, loader):
     lib = loader()
     names = declared(header)
@@ -33,6 +34,20 @@ def test_python_signatures_cover_header():
     assert declared("pbt.h") == set(N.SIGNATURES)
     assert declared("pbt_synth.h") == set(N.SYNTH_SIGNATURES)
     assert declared("pbt_probe.h") == set(N.PROBE_SIGNATURES)
+    from pascal_btdma_gb300 import batch
+
+    assert declared("pbt_batch.h") == set(batch.BATCH_SIGNATURES)
+
+
+def test_batch_create_rejects_without_gpu():
+    import numpy as np
+
+    from pascal_btdma_gb300 import batch
+
+    with pytest.raises(ValueError, match="m=7"):
+        batch.BatchPlan(np.array([2, 7]), np.array([10, 10]))
+    with pytest.raises(ValueError, match="equal length"):
+        batch.BatchPlan(np.array([2, 3]), np.array([10]))
 
 
 def test_version_and_partition():

@@ -67,3 +67,17 @@ def test_uneven_shapes():
     assert 6.5 < l.mean() < 8.5  # log-uniform on [4, 12]
     n2, m2 = synth.uneven_shapes(11, 32768)
     assert np.array_equal(n, n2) and np.array_equal(m, m2)
+
+
+def test_fill_batch_matches_uniform_fill():
+    """System s of a batch = system index s of a uniform batch with its shape."""
+    m = np.array([3, 3, 5, 2], dtype=np.int32)
+    n = np.array([7, 7, 4, 9], dtype=np.int32)
+    A, B, Cc, D, mo, vo = synth.fill_batch(m, n, seed=21, delta=1.3, nthreads=3)
+    for s in range(4):
+        u = synth.dominant(int(m[s]), s + 1, int(n[s]), seed=21, delta=1.3)
+        ms, ns = int(m[s]), int(n[s])
+        ua = u.A.reshape(ms * ms * ns, s + 1)[:, s]
+        ud = u.D.reshape(ms * ns, s + 1)[:, s]
+        assert np.array_equal(A[mo[s]:mo[s] + ms * ms * ns], ua)
+        assert np.array_equal(D[vo[s]:vo[s] + ms * ns], ud)
