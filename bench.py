@@ -422,7 +422,7 @@ def run_ours(args):
         p.destroy()
     del a, b, c, d0, hA, hB, hC, hD, keep, w, out_h
     torch.cuda.empty_cache()
-    for name, vm, vns, vn, vp, vdelta in VARIANTS:
+    for name, vm, vns, vn, vp, vdelta in (VARIANTS if "variants" in args.sections else []):
         vw, _ = make_workload(vm, vns, vn, vdelta, dev)
         va, vb, vc, vd = (torch.from_numpy(x).to(dev) for x in vw.arrays)
         vrows = vns * vn
@@ -450,7 +450,7 @@ def run_ours(args):
 
     mixed = {}
     by_delta = {}
-    for delta, nseg_m in MIXED:
+    for delta, nseg_m in (MIXED if "mixed" in args.sections else []):
         by_delta.setdefault(delta, []).append(nseg_m)
     for delta, segs in by_delta.items():
         mw, _ = make_workload(M, NSYS, NROW, delta, dev, row_scale=True)
@@ -482,58 +482,59 @@ def run_ours(args):
         torch.cuda.empty_cache()
 
     adjoint = {}
-    aw, _ = make_workload(ADJ["m"], ADJ["nsys"], ADJ["nrow"], ADJ["delta"], dev)
-    am, an, anr = ADJ["m"], ADJ["nsys"], ADJ["nrow"]
-    A0, B0, C0, D0 = (torch.from_numpy(x).to(dev) for x in aw.arrays)
+    if "adjoint" in args.sections:
+        aw, _ = make_workload(ADJ["m"], ADJ["nsys"], ADJ["nrow"], ADJ["delta"], dev)
+        am, an, anr = ADJ["m"], ADJ["nsys"], ADJ["nrow"]
+        A0, B0, C0, D0 = (torch.from_numpy(x).to(dev) for x in aw.arrays)
 
-    def time_adjoint(plan, A_, B_, C_, D_, m_, ns_, nr_, k):
-        x_ = D_.clone()
-        solve(plan, A_, B_, C_, x_, m_, ns_, nr_)
-        gsrc = torch.ones_like(D_)
-        da_, db_, dc_ = torch.empty_like(A_), torch.empty_like(B_), torch.empty_like(C_)
-        lam_ = gsrc.clone()
-        for _ in range(2):
-            lam_.copy_(gsrc)
-            pbt.adjoint_noncyclic(plan, A_, B_, C_, x_, lam_, da_, db_, dc_)
-        torch.cuda.synchronize()
-        bufs = [gsrc.clone() for _ in range(k)]
-        st_ = torch.cuda.current_stream()
-        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0_.record(st_)
-        for i_ in range(k):
-            pbt.adjoint_noncyclic(plan, A_, B_, C_, x_, bufs[i_], da_, db_, dc_)
-        e1_.record(st_)
-        torch.cuda.synchronize()
-        return e0_.elapsed_time(e1_) / 1e3 / k
+        def time_adjoint(plan, A_, B_, C_, D_, m_, ns_, nr_, k):
+            x_ = D_.clone()
+            solve(plan, A_, B_, C_, x_, m_, ns_, nr_)
+            gsrc = torch.ones_like(D_)
+            da_, db_, dc_ = torch.empty_like(A_), torch.empty_like(B_), torch.empty_like(C_)
+            lam_ = gsrc.clone()
+            for _ in range(2):
+                lam_.copy_(gsrc)
+                pbt.adjoint_noncyclic(plan, A_, B_, C_, x_, lam_, da_, db_, dc_)
+            torch.cuda.synchronize()
+            bufs = [gsrc.clone() for _ in range(k)]
+            st_ = torch.cuda.current_stream()
+            e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0_.record(st_)
+            for i_ in range(k):
+                pbt.adjoint_noncyclic(plan, A_, B_, C_, x_, bufs[i_], da_, db_, dc_)
+            e1_.record(st_)
+            torch.cuda.synchronize()
+            return e0_.elapsed_time(e1_) / 1e3 / k
 
-    for nseg_a in ADJ["segs"]:
-        for prec in ("ff", "fp64"):
-            with pbt.BtdmaGpuPlan() as pl:
-                pl.create(am, an, anr, nseg_a, precision=prec)
-                fs = time_device(pl, (A0, B0, C0), [D0], am, an, anr, 3, 3, ws, dev, solve) / 3
-                ad = time_adjoint(pl, A0, B0, C0, D0, am, an, anr, 3)
-            adjoint[f"{prec}_P{nseg_a}"] = {"forward_ms": fs * 1e3, "adjoint_ms": ad * 1e3,
-                                            "adjoint_over_forward": ad / fs,
-                                            "fused": nseg_a == 1 and am <= 6}
-    # memory pressure: 262144 systems, adjoint recomputes the factorisation
-    tiles = ADJ["pressure_tiles"]
-    ns_p = an * tiles
+        for nseg_a in ADJ["segs"]:
+            for prec in ("ff", "fp64"):
+                with pbt.BtdmaGpuPlan() as pl:
+                    pl.create(am, an, anr, nseg_a, precision=prec)
+                    fs = time_device(pl, (A0, B0, C0), [D0], am, an, anr, 3, 3, ws, dev, solve) / 3
+                    ad = time_adjoint(pl, A0, B0, C0, D0, am, an, anr, 3)
+                adjoint[f"{prec}_P{nseg_a}"] = {"forward_ms": fs * 1e3, "adjoint_ms": ad * 1e3,
+                                                "adjoint_over_forward": ad / fs,
+                                                "fused": nseg_a == 1 and am <= 6}
+        # memory pressure: 262144 systems, adjoint recomputes the factorisation
+        tiles = ADJ["pressure_tiles"]
+        ns_p = an * tiles
 
-    def tile(t, w_):
-        return t.view(-1, an).repeat(1, tiles).contiguous().view(-1)
+        def tile(t, w_):
+            return t.view(-1, an).repeat(1, tiles).contiguous().view(-1)
 
-    Ap, Bp, Cp, Dp = (tile(t, aw) for t in (A0, B0, C0, D0))
-    del A0, B0, C0, D0
-    with pbt.BtdmaGpuPlan() as pl:
-        pl.create(am, ns_p, anr, 1, precision="ff")
-        fs = time_device(pl, (Ap, Bp, Cp), [Dp], am, ns_p, anr, 2, 3, ws, dev, solve) / 2
-        ad = time_adjoint(pl, Ap, Bp, Cp, Dp, am, ns_p, anr, 2)
-    adjoint["ff_P1_nsys262144"] = {"forward_ms": fs * 1e3, "adjoint_ms": ad * 1e3,
-                                   "adjoint_over_forward": ad / fs, "fused": True,
-                                   "device_bytes_inputs": 8 * (3 * am * am + am) * ns_p * anr}
-    del Ap, Bp, Cp, Dp, aw
-    torch.cuda.empty_cache()
-    uneven = run_uneven(dev)
+        Ap, Bp, Cp, Dp = (tile(t, aw) for t in (A0, B0, C0, D0))
+        del A0, B0, C0, D0
+        with pbt.BtdmaGpuPlan() as pl:
+            pl.create(am, ns_p, anr, 1, precision="ff")
+            fs = time_device(pl, (Ap, Bp, Cp), [Dp], am, ns_p, anr, 2, 3, ws, dev, solve) / 2
+            ad = time_adjoint(pl, Ap, Bp, Cp, Dp, am, ns_p, anr, 2)
+        adjoint["ff_P1_nsys262144"] = {"forward_ms": fs * 1e3, "adjoint_ms": ad * 1e3,
+                                       "adjoint_over_forward": ad / fs, "fused": True,
+                                       "device_bytes_inputs": 8 * (3 * am * am + am) * ns_p * anr}
+        del Ap, Bp, Cp, Dp, aw
+        torch.cuda.empty_cache()
+    uneven = run_uneven(dev) if "uneven" in args.sections else {}
 
     result = {
         "metric": "block-rows/s (chosen method at <=1e-10 rel err vs plain FP64)",
@@ -574,7 +575,8 @@ def run_ours(args):
         "uneven_batch": uneven,
     }
     if rank == 0:
-        result["cpu_baseline"] = cpu_baseline(m, nrow, nseg, DELTA, target_s=args.cpu_seconds)
+        if "cpu" in args.sections:
+            result["cpu_baseline"] = cpu_baseline(m, nrow, nseg, DELTA, target_s=args.cpu_seconds)
         print(json.dumps(result), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -629,9 +631,21 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--sections", default="all",
+                    help="comma list of extra sections to run beside the headline: variants, mixed, adjoint, "
+                         "uneven, cpu; 'all' (default) or 'main' (headline only)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    known = {"variants", "mixed", "adjoint", "uneven", "cpu"}
+    if args.sections == "all":
+        args.sections = known
+    elif args.sections == "main":
+        args.sections = set()
+    else:
+        args.sections = set(args.sections.split(","))
+        if not args.sections <= known:
+            ap.error(f"unknown sections {sorted(args.sections - known)}")
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -68,7 +68,8 @@ typedef enum pbt_status {
     PBT_ESTATE = 3,       /* null or destroyed plan (std::runtime_error) */
     PBT_EUNSUPPORTED = 4, /* combination not provided (std::logic_error) */
     PBT_ENOMEM = 5,       /* device workspace allocation failed */
-    PBT_ESINGULAR = 6     /* a zero pivot was met in some block (pbt_plan_status) */
+    PBT_ESINGULAR = 6,    /* a zero pivot was met in some block (pbt_plan_status) */
+    PBT_ETIMEOUT = 7      /* a bounded device-side wait ran out (pbt_plan_status); results invalid */
 } pbt_status;
 
 /* Arithmetic of the solve. */
@@ -82,6 +83,10 @@ typedef enum pbt_precision {
 #define PBT_FLAG_CYCLIC 0x1u           /* periodic lines: plan for pbt_solve_cyclic */
 #define PBT_FLAG_INPLACE 0x2u          /* A, C receive the elimination factors; no factor workspace */
 #define PBT_FLAG_REFERENCE_METHOD 0x4u /* always run the two-stage (modified Thomas) method, even at nseg = 1 */
+#define PBT_FLAG_DIRECT_LOADS 0x8u     /* single-segment solve: always direct global loads */
+#define PBT_FLAG_STAGED_LOADS 0x10u    /* single-segment solve: TMA-staged loads wherever allowed (m <= 6,
+                                          nsys >= 32 and even, 16-byte aligned arrays) */
+/* Neither load flag: the library picks per solve (same results either way). */
 
 typedef struct pbt_plan_desc {
     int m;                 /* block size, 1..PBT_MAX_BLOCK */
@@ -193,7 +198,9 @@ int pbt_adjoint_noncyclic(pbt_plan* plan, const double* a, const double* b, cons
 /* Synchronises the plan's last stream and reports through *nsingular how
  * many zero pivots the solves since the previous call met (the reference has
  * no such report; its dgesv-less GPU path divides by zero silently).  Returns
- * PBT_ESINGULAR when *nsingular > 0.  nsingular may be NULL. */
+ * PBT_ETIMEOUT if a kernel's bounded wait for its staged input ran out (the
+ * solution of that solve is not valid), else PBT_ESINGULAR when
+ * *nsingular > 0.  nsingular may be NULL. */
 int pbt_plan_status(pbt_plan* plan, long long* nsingular);
 
 /* Outcome of the last solve on a PBT_PREC_FP32_REFINE plan: the number of

@@ -62,6 +62,10 @@ class SingularBlockError(ArithmeticError):
     """A zero pivot was met in some m x m block."""
 
 
+class DeviceWaitTimeout(RuntimeError):
+    """A kernel's bounded wait for its staged input ran out; the solve's result is not valid."""
+
+
 def _raise(code: int, where: str) -> None:
     if code == N.PBT_OK:
         return
@@ -78,6 +82,8 @@ def _raise(code: int, where: str) -> None:
         raise MemoryError(msg)
     if code == N.PBT_ESINGULAR:
         raise SingularBlockError(msg)
+    if code == N.PBT_ETIMEOUT:
+        raise DeviceWaitTimeout(msg)
     raise RuntimeError(f"{where}: status {code}: {N.last_error()}")
 
 
@@ -113,6 +119,8 @@ class BtdmaGpuPlan:
     cyclic: bool = False
     inplace: bool = False
     reference_method: bool = False
+    direct_loads: bool = False
+    staged_loads: bool = False
     created: bool = False
     _handle: C.c_void_p = field(default_factory=C.c_void_p, repr=False)
 
@@ -127,6 +135,8 @@ class BtdmaGpuPlan:
         cyclic: bool = False,
         inplace: bool = False,
         reference_method: bool = False,
+        direct_loads: bool = False,
+        staged_loads: bool = False,
         tol: float = 1e-12,
         max_iter: int = 8,
         threads_per_block: int = 0,
@@ -142,6 +152,8 @@ class BtdmaGpuPlan:
             (N.PBT_FLAG_CYCLIC if cyclic else 0)
             | (N.PBT_FLAG_INPLACE if inplace else 0)
             | (N.PBT_FLAG_REFERENCE_METHOD if reference_method else 0)
+            | (N.PBT_FLAG_DIRECT_LOADS if direct_loads else 0)
+            | (N.PBT_FLAG_STAGED_LOADS if staged_loads else 0)
         )
         d.tol = float(tol)
         d.max_iter = int(max_iter)
@@ -152,6 +164,7 @@ class BtdmaGpuPlan:
         self.m, self.nsys, self.nrow, self.nseg = d.m, d.nsys, d.nrow, d.nseg
         self.precision, self.cyclic, self.inplace = precision, cyclic, inplace
         self.reference_method = reference_method
+        self.direct_loads, self.staged_loads = direct_loads, staged_loads
         self.created = True
         return self
 

@@ -20,6 +20,7 @@ PBT_ESTATE = 3
 PBT_EUNSUPPORTED = 4
 PBT_ENOMEM = 5
 PBT_ESINGULAR = 6
+PBT_ETIMEOUT = 7
 
 PBT_PREC_FP64 = 0
 PBT_PREC_FF = 1
@@ -28,6 +29,8 @@ PBT_PREC_FP32_REFINE = 2
 PBT_FLAG_CYCLIC = 0x1
 PBT_FLAG_INPLACE = 0x2
 PBT_FLAG_REFERENCE_METHOD = 0x4
+PBT_FLAG_DIRECT_LOADS = 0x8
+PBT_FLAG_STAGED_LOADS = 0x10
 
 PBT_MAX_BLOCK = 10
 

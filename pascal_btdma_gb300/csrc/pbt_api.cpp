@@ -11,10 +11,14 @@
 //       into the reduced system) -> reduced solve (non-cyclic or cyclic) ->
 //       update.  The reference's two all-to-all exchanges have no
 //       counterpart: the reduced rows never leave device memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -39,6 +43,7 @@ int cuda_fail(cudaError_t e, const char* what) {
 struct pbt_plan {
     pbt_plan_desc desc;
     int device = 0;
+    int sms = 0;          // multiprocessors of `device`
     bool thomas = false;  // single-segment plain block Thomas path
     double* aw = nullptr;  // factor workspace (nullptr when in place)
     double* cw = nullptr;
@@ -166,6 +171,93 @@ cudaError_t run_accumulate(int m, const pbt::SolveArgs& g, double* X, const doub
 }
 
 PBT_DISPATCH(run_thomas, launch_thomas)
+
+#define PBT_DISPATCH_STAGED_M(NUM)                                         \
+    switch (m) {                                                           \
+        case 1: return pbt::launch_thomas_staged<NUM, 1>(g, maps);         \
+        case 2: return pbt::launch_thomas_staged<NUM, 2>(g, maps);         \
+        case 3: return pbt::launch_thomas_staged<NUM, 3>(g, maps);         \
+        case 4: return pbt::launch_thomas_staged<NUM, 4>(g, maps);         \
+        case 5: return pbt::launch_thomas_staged<NUM, 5>(g, maps);         \
+        case 6: return pbt::launch_thomas_staged<NUM, 6>(g, maps);         \
+        default: return cudaErrorNotSupported;                             \
+    }
+static_assert(pbt::kStagedMaxBlock == 6, "PBT_DISPATCH_STAGED_M lists block sizes 1..6");
+
+cudaError_t run_thomas_staged(int arith, int m, const pbt::SolveArgs& g, const pbt::ThomasMaps& maps) {
+    if (arith == kFF) {
+        PBT_DISPATCH_STAGED_M(pbt::FF)
+    }
+    if (arith == kF32) {
+        PBT_DISPATCH_STAGED_M(pbt::F32)
+    }
+    PBT_DISPATCH_STAGED_M(pbt::F64)
+}
+
+// cuTensorMapEncodeTiled, looked up once through the runtime (the library
+// links no driver library).  Null if the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// The {nsys, nrow, planes} FP64 tensor at `base` (reference layout), boxes of
+// one block column of 32 systems: {32, 1, m}.  False if the address or the
+// strides break the TMA rules (16-byte aligned base, strides multiples of 16
+// bytes, i.e. nsys even) or the driver refuses.
+bool encode_columns(CUtensorMap* tm, const double* base, int nsys, int nrow, int planes, int m) {
+    const PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+    if (fn == nullptr || base == nullptr || (reinterpret_cast<std::uintptr_t>(base) & 15u) != 0 || (nsys & 1))
+        return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)nsys, (cuuint64_t)nrow, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)nsys * 8u, (cuuint64_t)nsys * (cuuint64_t)nrow * 8u};
+    const cuuint32_t box[3] = {32u, 1u, (cuuint32_t)m};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    return fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launch the single-segment block Thomas solve, with TMA-staged loads
+// (k_thomas_staged) or direct loads (k_thomas); both give the same bits.
+// Staging wins where too few warps are resident to hide the loads' latency
+// -- batches of under 8 warps (256 systems) per SM -- and for the FP32
+// factorisation, which is bound by memory rather than arithmetic; with more
+// warps the direct kernel is a few percent faster (GB300, m = 5: float-float
+// 7.1 vs 7.2 ms on 65536 systems, 4.8 vs 7.2 ms staged on 16384).  The plan
+// flags force either; staging also needs m <= 6, nsys >= 32, nsys even and
+// 16-byte aligned arrays (the tensor-map rules), else direct loads run.
+cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveArgs& g) {
+    const pbt_plan_desc& ds = p->desc;
+    bool staged;
+    if (ds.flags & PBT_FLAG_DIRECT_LOADS)
+        staged = false;
+    else if (ds.flags & PBT_FLAG_STAGED_LOADS)
+        staged = true;
+    else
+        staged = arith == kF32 || p->sms <= 0 || (g.nsys + 31) / 32 < 8 * p->sms;
+    if (staged && m <= pbt::kStagedMaxBlock && g.nsys >= 32) {
+        pbt::ThomasMaps maps;
+        const int mm = m * m;
+        if (encode_columns(&maps.a, g.a, g.nsys, g.nrow, mm, m) && encode_columns(&maps.b, g.b, g.nsys, g.nrow, mm, m) &&
+            encode_columns(&maps.c, g.c, g.nsys, g.nrow, mm, m) && encode_columns(&maps.d, g.d, g.nsys, g.nrow, m, m) &&
+            encode_columns(&maps.w, g.cw, g.nsys, g.nrow, mm, m))
+            return run_thomas_staged(arith, m, g, maps);
+    }
+    return run_thomas(arith, m, g);
+}
+
 PBT_DISPATCH(run_modi, launch_modi)
 PBT_DISPATCH(run_reduced, launch_reduced)
 PBT_DISPATCH(run_reduced_cyclic, launch_reduced_cyclic)
@@ -214,8 +306,11 @@ int validate(const pbt_plan_desc& d) {
         (d.threads_per_block < 32 || d.threads_per_block > 128 || d.threads_per_block % 32 != 0)) {
         return fail(PBT_EINVAL, "plan: threads_per_block must be 0 or a multiple of 32 in 32..128");
     }
-    const unsigned known = PBT_FLAG_CYCLIC | PBT_FLAG_INPLACE | PBT_FLAG_REFERENCE_METHOD;
+    const unsigned known = PBT_FLAG_CYCLIC | PBT_FLAG_INPLACE | PBT_FLAG_REFERENCE_METHOD | PBT_FLAG_DIRECT_LOADS |
+                           PBT_FLAG_STAGED_LOADS;
     if (d.flags & ~known) return fail(PBT_EINVAL, "plan: unknown flag bits");
+    if ((d.flags & PBT_FLAG_DIRECT_LOADS) && (d.flags & PBT_FLAG_STAGED_LOADS))
+        return fail(PBT_EINVAL, "plan: PBT_FLAG_DIRECT_LOADS and PBT_FLAG_STAGED_LOADS exclude each other");
     return PBT_OK;
 }
 
@@ -311,7 +406,7 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
     double prev_ratio = 1.0;
     for (int it = 0; it < ds.max_iter; ++it) {
         if (p->thomas) {
-            e = run_thomas(kF32, m, make_args(p, a, b, c, p->re_, s, ds.nsys));
+            e = thomas_launch(p, kF32, m, make_args(p, a, b, c, p->re_, s, ds.nsys));
         } else {
             pbt::SolveArgs g = make_args(p, a, b, c, p->re_, s, ds.nsys * ds.nseg);
             e = run_modi(kF32, m, g);
@@ -377,7 +472,7 @@ int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
         for (int i = 1; i < 5; ++i)
             if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     } else if (p->thomas) {
-        e = run_thomas(arith_of(ds.precision), m, make_args(p, a, b, c, d, s, nsys));
+        e = thomas_launch(p, arith_of(ds.precision), m, make_args(p, a, b, c, d, s, nsys));
         if (e != cudaSuccess) return cuda_fail(e, "block Thomas launch");
         for (int i = 1; i < 5; ++i)
             if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
@@ -441,6 +536,10 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
     if (!p) return fail(PBT_ENOMEM, "plan_create: host allocation failed");
     p->desc = *desc;
     cudaGetDevice(&p->device);
+    if (cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
+        cudaGetLastError();
+        p->sms = 0;
+    }
     const auto& d = *desc;
     const bool inplace = (d.flags & PBT_FLAG_INPLACE) != 0;
     const bool cyclic = (d.flags & PBT_FLAG_CYCLIC) != 0;
@@ -534,7 +633,14 @@ int pbt_plan_status(pbt_plan* p, long long* nsingular) {
     if (e != cudaSuccess) return cuda_fail(e, "plan_status: read");
     e = cudaMemset(p->status, 0, sizeof v);
     if (e != cudaSuccess) return cuda_fail(e, "plan_status: reset");
+    const unsigned long long stalls = v / pbt::kStallMark;
+    v %= pbt::kStallMark;
     if (nsingular) *nsingular = (long long)v;
+    if (stalls) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "%llu bounded device wait(s) ran out; the solution is not valid", stalls);
+        return fail(PBT_ETIMEOUT, buf);
+    }
     if (v) return fail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
     return PBT_OK;
 }
@@ -583,7 +689,7 @@ int pbt_adjoint_noncyclic(pbt_plan* p, const double* a, const double* b, const d
     if ((e = run_transpose_blocks(m, g0, p->at, p->bt, p->ct)) != cudaSuccess)
         return cuda_fail(e, "adjoint: transpose launch");
     if (p->thomas) {
-        e = run_thomas(arith, m, make_args(p, p->at, p->bt, p->ct, g, s, ds.nsys));
+        e = thomas_launch(p, arith, m, make_args(p, p->at, p->bt, p->ct, g, s, ds.nsys));
         if (e != cudaSuccess) return cuda_fail(e, "adjoint: transposed solve launch");
     } else {
         pbt::SolveArgs gs = make_args(p, p->at, p->bt, p->ct, g, s, ds.nsys * ds.nseg);

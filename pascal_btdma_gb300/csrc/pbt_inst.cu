@@ -11,9 +11,15 @@
 #endif
 
 #include "pbt_kernels.cuh"
+#if PBT_M <= 6
+#include "pbt_staged.cuh"
+#endif
 
 namespace pbt {
 template cudaError_t launch_thomas<PBT_NUM, PBT_M>(const SolveArgs&);
+#if PBT_M <= 6
+template cudaError_t launch_thomas_staged<PBT_NUM, PBT_M>(const SolveArgs&, const ThomasMaps&);
+#endif
 template cudaError_t launch_modi<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_reduced<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_reduced_cyclic<PBT_NUM, PBT_M>(const SolveArgs&);

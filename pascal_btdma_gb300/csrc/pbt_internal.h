@@ -2,6 +2,7 @@
 // C ABI (pbt_api.cpp) and the per-block-size kernel objects (*_inst.cu).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -39,9 +40,24 @@ struct F64;
 struct FF;
 struct F32;
 
+// Tensor maps of the TMA-staged single-segment solve (pbt_staged.cuh): A, B,
+// C as {nsys, nrow, m*m} tensors, D as {nsys, nrow, m}, the factor
+// workspace (or C when in place) as {nsys, nrow, m*m}; every box is one block
+// column of 32 systems, {32, 1, m}.
+struct ThomasMaps {
+    CUtensorMap a, b, c, d, w;
+};
+// Largest block size with a staged kernel (larger blocks do not fit in the
+// registers of one thread anyway and keep the direct-load kernel).
+constexpr int kStagedMaxBlock = 6;
+// Added to a plan's status word (which otherwise counts zero pivots) by a
+// kernel whose bounded wait ran out.
+constexpr unsigned long long kStallMark = 1ull << 48;
+
 // Kernel launchers, explicitly instantiated per arithmetic and block size M
 // (1..PBT_MAX_BLOCK) in pbt_inst.cu.  Each returns cudaGetLastError().
 template <class Num, int M> cudaError_t launch_thomas(const SolveArgs& g);
+template <class Num, int M> cudaError_t launch_thomas_staged(const SolveArgs& g, const ThomasMaps& maps);
 template <class Num, int M> cudaError_t launch_modi(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced_cyclic(const SolveArgs& g);

@@ -138,6 +138,108 @@ PBT_UNROLL
 }
 
 // ---------------------------------------------------------------------------
+// The same elimination split in two.  lu_factor pivots and eliminates the
+// matrix alone and records what a right-hand side needs; lu_solve replays
+// that on one right-hand-side column.  Solving column by column holds the
+// factors plus one column in registers instead of the factors plus every
+// column, and each column sees exactly the operations of gesv<Num, M, NR>,
+// so the results are identical.  The multipliers stay where their row was
+// at their step (later swaps do not move them), which is what the in-order
+// replay in lu_solve needs.
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+struct LU {
+    static_assert(M <= 8, "LU::piv packs the M - 1 pivot rows in 4 bits each");
+    // f[k][c] (c > k): row k of U, normalised; f[i][k] (i > k): multiplier
+    // l_ik of step k; f[k][k]: 1 / U_kk.
+    typename Num::T f[M][M];
+    unsigned piv = 0;    // 4 bits per step k: the row swapped with row k
+    unsigned swaps = 0;  // bit k: some thread of the warp swapped at step k
+};
+
+template <class Num, int M>
+__device__ __forceinline__ void lu_factor(typename Num::Acc (&a)[M][M], LU<Num, M>& lu, bool& bad) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+PBT_UNROLL
+    for (int k = 0; k < M; ++k) {
+        if (k + 1 < M) {
+            int p = k;
+            auto best = Num::akey(a[k][k]);
+PBT_UNROLL
+            for (int i = k + 1; i < M; ++i) {
+                const auto v = Num::akey(a[i][k]);
+                const bool gt = v > best;
+                best = gt ? v : best;
+                p = gt ? i : p;
+            }
+            if (__any_sync(__activemask(), p != k)) {
+                lu.swaps |= 1u << k;
+PBT_UNROLL
+                for (int i = k + 1; i < M; ++i) {
+                    const unsigned s = (p == i);
+PBT_UNROLL
+                    for (int c = k; c < M; ++c) {
+                        const Acc t = a[k][c];
+                        a[k][c] = Num::asel(s, a[i][c], t);
+                        a[i][c] = Num::asel(s, t, a[i][c]);
+                    }
+                }
+            }
+            lu.piv |= static_cast<unsigned>(p) << (4 * k);
+        }
+        const T pv = Num::fin(a[k][k]);
+        bad |= Num::is_zero(pv);
+        const T r = Num::rcp(pv);
+        lu.f[k][k] = r;
+        T uk[M];
+PBT_UNROLL
+        for (int c = k + 1; c < M; ++c) {
+            uk[c] = Num::fin(a[k][c]);
+            lu.f[k][c] = uk[c];
+        }
+PBT_UNROLL
+        for (int i = k + 1; i < M; ++i) {
+            const T l = Num::mul(Num::fin(a[i][k]), r);
+            lu.f[i][k] = l;
+PBT_UNROLL
+            for (int c = k + 1; c < M; ++c) Num::msub(a[i][c], l, uk[c]);
+        }
+    }
+}
+
+// x = a^{-1} b for one column b (consumed) with the factors of lu_factor.
+template <class Num, int M>
+__device__ __forceinline__ void lu_solve(const LU<Num, M>& lu, typename Num::Acc (&b)[M], typename Num::T (&x)[M]) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+PBT_UNROLL
+    for (int k = 0; k < M; ++k) {
+        if (k + 1 < M && ((lu.swaps >> k) & 1u)) {
+            const unsigned p = (lu.piv >> (4 * k)) & 15u;
+PBT_UNROLL
+            for (int i = k + 1; i < M; ++i) {
+                const unsigned s = (p == static_cast<unsigned>(i));
+                const Acc t = b[k];
+                b[k] = Num::asel(s, b[i], t);
+                b[i] = Num::asel(s, t, b[i]);
+            }
+        }
+        const T bk = Num::fin(b[k]);
+        b[k] = Num::acc(bk);
+PBT_UNROLL
+        for (int i = k + 1; i < M; ++i) Num::msub(b[i], lu.f[i][k], bk);
+    }
+PBT_UNROLL
+    for (int k = M - 1; k >= 0; --k) {
+        const T xk = Num::mul(Num::fin(b[k]), lu.f[k][k]);
+        x[k] = xk;
+PBT_UNROLL
+        for (int i = 0; i < k; ++i) Num::msub(b[i], lu.f[i][k], xk);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Loads and stores of one block / vector at `base` (= X + sys + nsys*row).
 // ---------------------------------------------------------------------------
 template <class Num, int M>
@@ -317,13 +419,150 @@ PBT_UNROLL
     }
 }
 
+// Block Thomas with the row step split into factor and column solves
+// (lu_factor / lu_solve), for the register-resident block sizes.  The
+// previous row's C' lives in shared memory (`cps`: this thread's M*M raw
+// values, element (k, j) at cps[(k*M + j) * cstride]) instead of registers:
+// the row reads it one row k at a time, so the registers hold the row's
+// accumulators, the factors and one column, not also C'_{q-1} and every
+// right-hand side.  With Num::kAddBLast, R_q = -A_q C'_{q-1} + B_q is
+// accumulated from zero with B added last; otherwise from B, as thomas_body.
+// The operations and their order are exactly those of the TMA-staged kernel
+// k_thomas_staged, so the two agree bit for bit.
+template <class Num, int M>
+__device__ __forceinline__ void thomas_body_lu(const double* A, const double* B, const double* C, double* D,
+                                               double* CW, double* cps, int cstride, size_t plane0, size_t rs,
+                                               int N, bool raw, bool& bad) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    // Element e = i + M*j of a row's block is at base + e*plane: every phase
+    // walks its array in increasing e with one running pointer, and re-reads
+    // the plane stride through opaque() so that no phase keeps a table of
+    // 64-bit element addresses alive across the arithmetic.
+    T y[M];
+    for (int q = 0; q < N; ++q) {
+        const size_t o = (size_t)q * rs;
+        const bool last = (q == N - 1);
+        Acc r[M][M], xd[M];
+        {
+            const size_t plane = opaque(plane0);
+            const double* pd = D + o;
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pd += plane) xd[i] = Num::acc(Num::in(pd));
+        }
+        // R = B - A C'_{q-1}: from B (Num::kAddBLast false) or from zero with
+        // B added last, in the order the staged kernel receives the blocks.
+        auto add_b = [&]() {
+            const size_t plane = opaque(plane0);
+            const double* pb = B + o;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pb += plane) {
+                    const T b = Num::in_ro(pb);
+                    if constexpr (Num::kAddBLast)
+                        Num::add(r[i][j], b);
+                    else
+                        r[i][j] = Num::acc(b);
+                }
+        };
+        if constexpr (Num::kAddBLast) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) r[i][j] = Num::acc0();
+        } else {
+            add_b();
+        }
+        if (q > 0) {
+            const size_t plane = opaque(plane0);
+            const double* pa = A + o;
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) {
+                T ck[M];
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ck[j] = Num::lds(cps + (k * M + j) * cstride);
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) {
+                    const T a = Num::in(pa);
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
+                    Num::msub(xd[i], a, y[k]);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+        if constexpr (Num::kAddBLast) add_b();
+        LU<Num, M> lu;
+        lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, xd, y);
+        {
+            const size_t plane = opaque(plane0);
+            if (last) {
+                out_vec<Num, M>(D + o, plane, y);
+                break;
+            }
+            st_raw_vec<Num, M>(D + o, plane, y);
+        }
+        const size_t plane = opaque(plane0);
+        const double* pc = C + o;
+        double* pw = CW + o;
+PBT_UNROLL
+        for (int j = 0; j < M; ++j) {
+            Acc cj[M];
+            T xj[M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pc += plane) cj[i] = Num::acc(Num::in(pc));
+            lu_solve<Num, M>(lu, cj, xj);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pw += plane) {
+                if (raw || !Num::kConv)
+                    Num::sts(pw, xj[i]);
+                else
+                    Num::out(pw, xj[i]);
+                Num::sts(cps + (i * M + j) * cstride, xj[i]);
+            }
+            if (PBT_ROW_FENCE) mem_fence_compiler();
+        }
+    }
+    for (int q = N - 2; q >= 0; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T c[M][M], t[M];
+        ld_fac_blk<Num, M>(c, CW + o, plane, raw);
+        ld_raw_vec<Num, M>(t, D + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+            t[i] = Num::fin(s);
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) y[i] = t[i];
+        out_vec<Num, M>(D + o, plane, y);
+    }
+}
+
+// Block sizes whose single-segment solve keeps its blocks in registers and
+// parks C'_{q-1} in shared memory (thomas_body_lu); larger blocks use
+// thomas_body with local memory.
+constexpr int kThomasLuMaxBlock = 6;
+
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
     if (sys >= g.nsys) return;
     bool bad = false;
-    thomas_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
-                        (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
+    if constexpr (M <= kThomasLuMaxBlock) {
+        extern __shared__ double thomas_cps[];
+        thomas_body_lu<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, thomas_cps + threadIdx.x,
+                               blockDim.x, (size_t)g.nsys * g.nrow, (size_t)g.nsys, g.nrow, g.factors_raw != 0,
+                               bad);
+    } else {
+        thomas_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
+                            (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
+    }
     if (bad) atomicAdd(g.status, 1ull);
 }
 
@@ -1118,7 +1357,8 @@ inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) /
 template <class Num, int M>
 cudaError_t launch_thomas(const SolveArgs& g) {
     const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
-    k_thomas<Num, M><<<grid_x(g.nsys, tpb), tpb, 0, g.stream>>>(g);
+    const size_t smem = M <= kThomasLuMaxBlock ? (size_t)tpb * M * M * sizeof(double) : 0;
+    k_thomas<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g);
     return cudaGetLastError();
 }
 template <class Num, int M>

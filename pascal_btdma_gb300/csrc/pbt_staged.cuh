@@ -1,0 +1,430 @@
+// pbt_staged.cuh -- the single-segment block Thomas solve with its inputs
+// staged through shared memory by the Tensor Memory Accelerator.
+//
+// Why: one thread carries one system's whole block row, and a 65536-system
+// batch has only 2048 warps -- 13.5 per SM -- so the direct-load kernel
+// (k_thomas) waits on global loads it cannot issue early enough (a row's
+// inputs are 3m^2 + m doubles, more than its register budget).  Here the
+// loads are asynchronous bulk tensor copies (cp.async.bulk.tensor) into a
+// ring of shared-memory slots, issued one ring ahead of use, and the
+// arithmetic reads shared memory.
+//
+// Shape: one warp per CTA, one system per lane, 32 consecutive systems per
+// CTA.  A ring item is one block COLUMN of one array for the CTA's 32 systems:
+// elements (0..m-1, j) of row q, which in the reference layout
+// X[sys + nsys*(row + nrow*(i + m*j))] is the 3-D box {32 systems, 1 row,
+// m planes} at (s0, q, j*m) of the tensor {nsys, nrow, planes}.  In shared
+// memory the box lands as slot[i][lane], so lane l reads its column from
+// slot + l + 32*i without bank conflicts.
+//
+// Item order, forward sweep (row q): d_q, A_q and B_q columns 0..m-1 (see
+// fwd_item), C_q columns -- the order the row consumes them: R = B - A C'_{q-1}
+// and rhs = d - A y_{q-1} are accumulated column by column of A (C'_{q-1}
+// read from shared memory one row at a time), R is factorised (lu_factor), and
+// y_q and the columns of C'_q are solved one at a time (lu_solve), each
+// C'_q column going to the factor workspace and to shared memory for the
+// next row.  A_0 and C_{nrow-1} are fetched and ignored, so every row has the
+// same 1 + 3m items.  Backward sweep (row q = nrow-2 .. 0): C'_q columns
+// 0..m-1 from the factor workspace, then y_q.  The arithmetic, and so every
+// result bit, is that of the direct-load kernel k_thomas.
+//
+// Ring protocol: R slots, one mbarrier each.  Item n uses slot n % R and
+// completes phase (n / R) & 1 of its barrier.  Lane 0 issues item n + R into
+// the slot of item n as soon as every lane has read item n (__syncwarp), so
+// each copy has R items of arithmetic to land in.  Between the sweeps every
+// lane fences its generic-proxy global stores (C'_q, y_q) against the
+// async-proxy reads of the backward sweep.  Every wait is bounded (2 s on
+// the global timer); a wait that runs out adds kStallMark to the status word,
+// stops issuing, waits (bounded) for the copies already in flight and ends
+// the CTA.
+#pragma once
+
+#include <cuda.h>
+
+#include "pbt_kernels.cuh"
+
+namespace pbt {
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
+
+static __device__ __noinline__ bool mbar_wait_slow(unsigned bar, unsigned parity, unsigned long long limit_ns) {
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    return mbar_try_wait(bar, parity) || mbar_wait_slow(bar, parity, kWaitLimitNs);
+}
+// 3-D tile load of `map` at (x, y, z) into shared memory, completing on `bar`.
+// x (the system index) is a multiple of 32, so x * 8 bytes is 16-byte aligned.
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap* map, int x, int y, int z, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+// Shared memory of one CTA: the ring (R items of M*32 doubles) and C'_{q-1}
+// (M*M*32 raw values).  Sized so that 15 one-warp CTAs fit in an SM
+// (15 * (14 KB + 1 KB reserved) <= 228 KB): 15 * 152 = 2280 resident warps
+// cover a 65536-system batch (2048 warps) in one wave.
+constexpr int kStagedSmemBudget = 14336;
+template <int M>
+__host__ __device__ constexpr int staged_ring() {
+    return (kStagedSmemBudget - M * M * 256) / (M * 256 + 8) < 4 ? 4
+           : (kStagedSmemBudget - M * M * 256) / (M * 256 + 8) > 3 * (1 + 3 * M)
+               ? 3 * (1 + 3 * M)
+               : (kStagedSmemBudget - M * M * 256) / (M * 256 + 8);
+}
+template <int M>
+__host__ __device__ constexpr int staged_smem_bytes() {
+    return (staged_ring<M>() * M + M * M) * 32 * 8;
+}
+
+// Forward item k of a row: which array and which plane offset.  Items:
+// d_q, then the A and the B columns -- A first when the arithmetic adds B
+// last (Num::kAddBLast), B first otherwise -- then the C columns.  With A
+// first every item has at least one block column of arithmetic between its
+// issue and its use, even with the 6-item ring of m = 5; with B first the A
+// columns are issued while the (instant) B reads run, and each row starts
+// with a memory latency, which the FP64 solve, bound by its FP64 pipe, hides.
+template <class Num, int M>
+__device__ __forceinline__ const CUtensorMap* fwd_item(const ThomasMaps& mp, int k, int& z) {
+    if (k == 0) {
+        z = 0;
+        return &mp.d;
+    }
+    if (k <= M) {
+        z = (k - 1) * M;
+        return Num::kAddBLast ? &mp.a : &mp.b;
+    }
+    if (k <= 2 * M) {
+        z = (k - 1 - M) * M;
+        return Num::kAddBLast ? &mp.b : &mp.a;
+    }
+    z = (k - 1 - 2 * M) * M;
+    return &mp.c;
+}
+// Backward item k of a row: C'_q column k (k < M) or y_q (k == M).
+template <int M>
+__device__ __forceinline__ const CUtensorMap* bwd_item(const ThomasMaps& mp, int k, int& z) {
+    if (k < M) {
+        z = k * M;
+        return &mp.w;
+    }
+    z = 0;
+    return &mp.d;
+}
+
+template <class Num>
+__device__ __forceinline__ typename Num::T fac_in(const double* p, bool raw) {
+    return (raw || !Num::kConv) ? Num::lds(p) : Num::in(p);
+}
+
+// Resident one-warp CTAs per SM the register budget is sized for (16: at most
+// 128 registers a thread; shared memory allows 15).
+#ifndef PBT_STAGED_MIN_CTAS
+#define PBT_STAGED_MIN_CTAS 16
+#endif
+
+template <class Num, int M>
+__global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const __grid_constant__ ThomasMaps maps, const SolveArgs g) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    constexpr int R = staged_ring<M>();
+    constexpr int K = 1 + 3 * M;  // forward items per row
+    constexpr int K2 = M + 1;     // backward items per row
+    constexpr unsigned kSlotBytes = M * 32 * 8;
+    extern __shared__ __align__(128) double ring[];
+    __shared__ __align__(8) unsigned long long bars[R];
+
+    const int lane = threadIdx.x;
+    const int s0 = blockIdx.x * 32;
+    const bool active = s0 + lane < g.nsys;
+    const int N = g.nrow;
+    const size_t plane0 = (size_t)g.nsys * N;
+    const bool raw = g.factors_raw != 0;
+    const unsigned ring_s = smem_u32(ring), bar_s = smem_u32(bars);
+    double* const D = g.d + s0 + lane;
+    double* const CW = g.cw + s0 + lane;
+
+    if (lane == 0) {
+        for (int j = 0; j < R; ++j) mbar_init(bar_s + 8u * j, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+
+    // Consumer position: the next item's slot and barrier phase, and how many
+    // items of the whole sequence (forward, then backward) were consumed.
+    int slot = 0;
+    unsigned phase = 0;
+    int n_cons = 0;
+    bool ok = true;
+
+    auto issue = [&](int s, const CUtensorMap* map, int row, int z) {
+        mbar_expect_tx(bar_s + 8u * s, kSlotBytes);
+        tma_load_3d(ring_s + kSlotBytes * s, map, s0, row, z, bar_s + 8u * s);
+    };
+    auto take = [&]() -> const double* {
+        if (ok) ok = __all_sync(0xffffffffu, mbar_wait(bar_s + 8u * slot, phase));
+        return ring + slot * (M * 32) + lane;
+    };
+    // Release the current item and refill its slot with the item R later
+    // (map == nullptr: the sequence of this sweep has ended).
+    auto give = [&](const CUtensorMap* map, int row, int z) {
+        if (!ok) return;
+        __syncwarp();
+        if (lane == 0 && map != nullptr) {
+            fence_proxy_async_shared();
+            issue(slot, map, row, z);
+        }
+        ++n_cons;
+        if (++slot == R) {
+            slot = 0;
+            phase ^= 1u;
+        }
+    };
+    // Item R positions after item k of forward row q.
+    auto fwd_next = [&](int q, int k, int& row, int& z) -> const CUtensorMap* {
+        const int kk = k + R;
+        row = q + kk / K;
+        return row < N ? fwd_item<Num, M>(maps, kk % K, z) : nullptr;
+    };
+    auto bwd_next = [&](int b, int k, int& row, int& z) -> const CUtensorMap* {
+        const int kk = k + R;
+        const int bb = b + kk / K2;
+        row = N - 2 - bb;
+        return bb < N - 1 ? bwd_item<M>(maps, kk % K2, z) : nullptr;
+    };
+
+    if (lane == 0) {
+        for (int j = 0; j < R && j < N * K; ++j) {
+            int z;
+            const CUtensorMap* mp = fwd_item<Num, M>(maps, j % K, z);
+            issue(j, mp, j / K, z);
+        }
+    }
+
+    bool bad = false;
+    T y[M];
+    double* const cps = ring + R * M * 32 + lane;  // this lane's C'_{q-1}: (k, j) at cps[32 * (k*M + j)]
+    for (int q = 0; q < N; ++q) {
+        const size_t o = (size_t)q * g.nsys;
+        const bool last = (q == N - 1);
+        Acc r[M][M], xd[M];
+        int nrow_, nz;
+        {
+            const double* p = take();
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) xd[i] = Num::acc(Num::in(p + 32 * i));
+            const CUtensorMap* nm = fwd_next(q, 0, nrow_, nz);
+            give(nm, nrow_, nz);
+        }
+        // Items 1..2M: the A and B columns in the order fwd_item gives.
+        auto a_cols = [&](int k0) {
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) {
+                const double* p = take();
+                if (q > 0) {
+                    T ck[M];
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) ck[j] = Num::lds(cps + 32 * (k * M + j));
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) {
+                        const T a = Num::in(p + 32 * i);
+PBT_UNROLL
+                        for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
+                        Num::msub(xd[i], a, y[k]);
+                    }
+                }
+                const CUtensorMap* nm = fwd_next(q, k0 + k, nrow_, nz);
+                give(nm, nrow_, nz);
+            }
+        };
+        auto b_cols = [&](int k0) {
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) {
+                const double* p = take();
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) {
+                    const T b = Num::in(p + 32 * i);
+                    if constexpr (Num::kAddBLast)
+                        Num::add(r[i][j], b);
+                    else
+                        r[i][j] = Num::acc(b);
+                }
+                const CUtensorMap* nm = fwd_next(q, k0 + j, nrow_, nz);
+                give(nm, nrow_, nz);
+            }
+        };
+        if constexpr (Num::kAddBLast) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) r[i][j] = Num::acc0();
+            a_cols(1);
+            b_cols(1 + M);
+        } else {
+            b_cols(1);
+            a_cols(1 + M);
+        }
+        LU<Num, M> lu;
+        lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, xd, y);
+        {
+            const size_t plane = opaque(plane0);
+            if (!last) {
+                if (active && ok) st_raw_vec<Num, M>(D + o, plane, y);
+            } else {
+                if (active && ok) out_vec<Num, M>(D + o, plane, y);
+            }
+        }
+        const size_t plane = opaque(plane0);
+        double* pw = CW + o;
+PBT_UNROLL
+        for (int j = 0; j < M; ++j) {
+            const double* p = take();
+            if (!last) {
+                Acc cj[M];
+                T xj[M];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) cj[i] = Num::acc(Num::in(p + 32 * i));
+                lu_solve<Num, M>(lu, cj, xj);
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pw += plane) {
+                    if (active && ok) {
+                        if (raw || !Num::kConv)
+                            Num::sts(pw, xj[i]);
+                        else
+                            Num::out(pw, xj[i]);
+                    }
+                    Num::sts(cps + 32 * (i * M + j), xj[i]);
+                }
+            }
+            const CUtensorMap* nm = fwd_next(q, 1 + 2 * M + j, nrow_, nz);
+            give(nm, nrow_, nz);
+        }
+        if (!ok) break;
+    }
+
+    int n_end = N * K;  // end of the sweep in progress (items)
+    if (ok) {
+        // The backward sweep reads, through the async proxy, what this warp's
+        // lanes just stored through the generic proxy.
+        fence_proxy_async_global();
+        __syncwarp();
+        n_end = N * K + (N - 1) * K2;
+        if (lane == 0) {
+            for (int j = 0; j < R && j < (N - 1) * K2; ++j) {
+                int z;
+                const CUtensorMap* mp = bwd_item<M>(maps, j % K2, z);
+                const int s = (slot + j) % R;
+                issue(s, mp, N - 2 - j / K2, z);
+            }
+        }
+        for (int b = 0; b < N - 1; ++b) {
+            const int q = N - 2 - b;
+            const size_t o = (size_t)q * g.nsys;
+            T c[M][M], t[M];
+            int nrow_, nz;
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) {
+                const double* p = take();
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) c[i][k] = fac_in<Num>(p + 32 * i, raw);
+                const CUtensorMap* nm = bwd_next(b, k, nrow_, nz);
+                give(nm, nrow_, nz);
+            }
+            {
+                const double* p = take();
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) t[i] = Num::lds(p + 32 * i);
+                const CUtensorMap* nm = bwd_next(b, M, nrow_, nz);
+                give(nm, nrow_, nz);
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                Acc s = Num::acc(t[i]);
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+                t[i] = Num::fin(s);
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) y[i] = t[i];
+            if (active && ok) out_vec<Num, M>(D + o, plane0, y);
+            if (!ok) break;
+        }
+    }
+
+    if (!ok) {
+        // A wait ran out: report it, then wait (boundedly) for the copies
+        // still in flight -- items n_cons .. n_cons+R-1 of the current sweep --
+        // so none lands in shared memory after the CTA has ended.
+        if (lane == 0) {
+            atomicAdd(g.status, kStallMark);
+            int s = slot;
+            unsigned ph = phase;
+            for (int j = 0; j < R && n_cons + j < n_end; ++j) {
+                if (!mbar_try_wait(bar_s + 8u * s, ph)) mbar_wait_slow(bar_s + 8u * s, ph, kWaitLimitNs / 4);
+                if (++s == R) {
+                    s = 0;
+                    ph ^= 1u;
+                }
+            }
+        }
+        __syncwarp();
+        return;
+    }
+    if (bad && active) atomicAdd(g.status, 1ull);
+}
+
+template <class Num, int M>
+cudaError_t launch_thomas_staged(const SolveArgs& g, const ThomasMaps& maps) {
+    if (M > kStagedMaxBlock) return cudaErrorNotSupported;
+    constexpr int smem = staged_smem_bytes<M>();
+    static bool configured = false;  // per instantiation; idempotent, so a race is harmless
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_thomas_staged<Num, M>,
+                                             cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    const unsigned grid = (unsigned)((g.nsys + 31) / 32);
+    k_thomas_staged<Num, M><<<grid, 32, smem, g.stream>>>(maps, g);
+    return cudaGetLastError();
+}
+
+}  // namespace pbt

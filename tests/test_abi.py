@@ -39,6 +39,19 @@ def test_python_signatures_cover_header():
     assert declared("pbt_batch.h") == set(batch.BATCH_SIGNATURES)
 
 
+def test_python_constants_match_header():
+    """Status codes, precisions and flags in the ctypes layer equal pbt.h's."""
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "pbt.h").read_text(), flags=re.S)
+    found = {}
+    for name, val in re.findall(r"\b(PBT_[A-Z0-9_]+)\s*=\s*(\d+)", text):
+        found[name] = int(val)
+    for name, val in re.findall(r"#define\s+(PBT_FLAG_[A-Z_]+)\s+0x([0-9a-fA-F]+)u", text):
+        found[name] = int(val, 16)
+    assert {"PBT_ETIMEOUT", "PBT_ESINGULAR", "PBT_PREC_FF", "PBT_FLAG_DIRECT_LOADS"} <= set(found)
+    for name, val in found.items():
+        assert getattr(N, name) == val, name
+
+
 def test_batch_create_rejects_without_gpu():
     import numpy as np
 
@@ -90,6 +103,7 @@ def create(**kw):
         (dict(nrow=10, nseg=4), N.PBT_EINVAL, ">= 3 rows"),
         (dict(flags=N.PBT_FLAG_CYCLIC), N.PBT_EINVAL, "cyclic"),
         (dict(flags=0x100), N.PBT_EINVAL, "unknown flag"),
+        (dict(flags=N.PBT_FLAG_DIRECT_LOADS | N.PBT_FLAG_STAGED_LOADS), N.PBT_EINVAL, "exclude each other"),
         (dict(threads_per_block=48), N.PBT_EINVAL, "threads_per_block"),
         (dict(precision=7), N.PBT_EUNSUPPORTED, "precision"),
         (dict(precision=N.PBT_PREC_FP32_REFINE, flags=N.PBT_FLAG_INPLACE), N.PBT_EINVAL, "unchanged"),
