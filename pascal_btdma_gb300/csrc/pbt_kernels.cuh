@@ -33,7 +33,7 @@
 // caller's A and C are converted to FP64 so those arrays stay valid doubles.
 #pragma once
 
-#include "pbt_block64.cuh"
+#include "pbt_util.cuh"
 #include "pbt_internal.h"
 #include "pbt_num.cuh"
 
@@ -57,7 +57,11 @@ __device__ __forceinline__ void seg_rows(int n, int p, int s, int& first, int& l
 
 // ---------------------------------------------------------------------------
 // Gaussian elimination with partial pivoting on [a | b] (M x M, M x NR);
-// the solution a^{-1} b is left in b.  Pivot = first row of maximal |a(i,k)|
+// the solution a^{-1} b is left in b.  This is the block solve of the
+// reference GPU path (gesv / gesv_mrhs2 / gesv_mrhs3,
+// Fortran_Original/src/mod_btdma_gpu_v2.f90:921-1123, which does not pivot)
+// with the partial pivoting of the reference CPU path's LAPACK dgesv
+// (Fortran_Original/src/mod_btdma_cpu.f90:339,357,381,421).  Pivot = first row of maximal |a(i,k)|
 // (LAPACK idamax rule; for FF the high part decides); multipliers are
 // a(i,k) * (1/a(k,k)) as in dgetf2.  Entries are accumulators, normalised
 // only when their row becomes the pivot row.  A zero pivot sets `bad`; the
@@ -419,13 +423,36 @@ PBT_UNROLL
     }
 }
 
+// Which body the direct-load single-segment kernel runs per block size:
+// thomas_body (fused gesv, every right-hand side in registers) for m <= 4,
+// where that fits the register budget and is the fastest form (GB300,
+// float-float m = 4, 131072 systems: 14.8 ms vs 17.0 ms split); thomas_body_lu
+// for m = 5, 6 (float-float m = 5, 65536 systems: 7.1 ms vs 8.6 ms fused);
+// thomas_body with local-memory blocks above.
+#ifndef PBT_THOMAS_LU_MIN
+#define PBT_THOMAS_LU_MIN 5
+#endif
+constexpr int kThomasLuMinBlock = PBT_THOMAS_LU_MIN;
+constexpr int kThomasLuMaxBlock = 6;
+template <int M>
+__host__ __device__ constexpr bool thomas_uses_lu() {
+    return M >= kThomasLuMinBlock && M <= kThomasLuMaxBlock;
+}
+// Whether a row accumulates R = -A C'_{q-1} from zero and adds B last
+// (Num::kAddBLast) -- only in the split form; the fused form starts from B.
+// The staged kernel follows the same rule, so both give the same bits.
+template <class Num, int M>
+__host__ __device__ constexpr bool thomas_b_last() {
+    return Num::kAddBLast && thomas_uses_lu<M>();
+}
+
 // Block Thomas with the row step split into factor and column solves
 // (lu_factor / lu_solve), for the register-resident block sizes.  The
 // previous row's C' lives in shared memory (`cps`: this thread's M*M raw
 // values, element (k, j) at cps[(k*M + j) * cstride]) instead of registers:
 // the row reads it one row k at a time, so the registers hold the row's
 // accumulators, the factors and one column, not also C'_{q-1} and every
-// right-hand side.  With Num::kAddBLast, R_q = -A_q C'_{q-1} + B_q is
+// right-hand side.  With thomas_b_last, R_q = -A_q C'_{q-1} + B_q is
 // accumulated from zero with B added last; otherwise from B, as thomas_body.
 // The operations and their order are exactly those of the TMA-staged kernel
 // k_thomas_staged, so the two agree bit for bit.
@@ -450,7 +477,7 @@ __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B,
 PBT_UNROLL
             for (int i = 0; i < M; ++i, pd += plane) xd[i] = Num::acc(Num::in(pd));
         }
-        // R = B - A C'_{q-1}: from B (Num::kAddBLast false) or from zero with
+        // R = B - A C'_{q-1}: from B (thomas_b_last false) or from zero with
         // B added last, in the order the staged kernel receives the blocks.
         auto add_b = [&]() {
             const size_t plane = opaque(plane0);
@@ -460,13 +487,13 @@ PBT_UNROLL
 PBT_UNROLL
                 for (int i = 0; i < M; ++i, pb += plane) {
                     const T b = Num::in_ro(pb);
-                    if constexpr (Num::kAddBLast)
+                    if constexpr (thomas_b_last<Num, M>())
                         Num::add(r[i][j], b);
                     else
                         r[i][j] = Num::acc(b);
                 }
         };
-        if constexpr (Num::kAddBLast) {
+        if constexpr (thomas_b_last<Num, M>()) {
 PBT_UNROLL
             for (int i = 0; i < M; ++i)
 PBT_UNROLL
@@ -492,7 +519,7 @@ PBT_UNROLL
                 if (PBT_ROW_FENCE) mem_fence_compiler();
             }
         }
-        if constexpr (Num::kAddBLast) add_b();
+        if constexpr (thomas_b_last<Num, M>()) add_b();
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
         lu_solve<Num, M>(lu, xd, y);
@@ -544,17 +571,13 @@ PBT_UNROLL
     }
 }
 
-// Block sizes whose single-segment solve keeps its blocks in registers and
-// parks C'_{q-1} in shared memory (thomas_body_lu); larger blocks use
-// thomas_body with local memory.
-constexpr int kThomasLuMaxBlock = 6;
 
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
     if (sys >= g.nsys) return;
     bool bad = false;
-    if constexpr (M <= kThomasLuMaxBlock) {
+    if constexpr (thomas_uses_lu<M>()) {
         extern __shared__ double thomas_cps[];
         thomas_body_lu<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, thomas_cps + threadIdx.x,
                                blockDim.x, (size_t)g.nsys * g.nrow, (size_t)g.nsys, g.nrow, g.factors_raw != 0,
@@ -1357,7 +1380,7 @@ inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) /
 template <class Num, int M>
 cudaError_t launch_thomas(const SolveArgs& g) {
     const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
-    const size_t smem = M <= kThomasLuMaxBlock ? (size_t)tpb * M * M * sizeof(double) : 0;
+    const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * M * M * sizeof(double) : 0;
     k_thomas<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g);
     return cudaGetLastError();
 }

@@ -115,7 +115,7 @@ __host__ __device__ constexpr int staged_smem_bytes() {
 
 // Forward item k of a row: which array and which plane offset.  Items:
 // d_q, then the A and the B columns -- A first when the arithmetic adds B
-// last (Num::kAddBLast), B first otherwise -- then the C columns.  With A
+// last (thomas_b_last), B first otherwise -- then the C columns.  With A
 // first every item has at least one block column of arithmetic between its
 // issue and its use, even with the 6-item ring of m = 5; with B first the A
 // columns are issued while the (instant) B reads run, and each row starts
@@ -128,11 +128,11 @@ __device__ __forceinline__ const CUtensorMap* fwd_item(const ThomasMaps& mp, int
     }
     if (k <= M) {
         z = (k - 1) * M;
-        return Num::kAddBLast ? &mp.a : &mp.b;
+        return thomas_b_last<Num, M>() ? &mp.a : &mp.b;
     }
     if (k <= 2 * M) {
         z = (k - 1 - M) * M;
-        return Num::kAddBLast ? &mp.b : &mp.a;
+        return thomas_b_last<Num, M>() ? &mp.b : &mp.a;
     }
     z = (k - 1 - 2 * M) * M;
     return &mp.c;
@@ -280,7 +280,7 @@ PBT_UNROLL
 PBT_UNROLL
                 for (int i = 0; i < M; ++i) {
                     const T b = Num::in(p + 32 * i);
-                    if constexpr (Num::kAddBLast)
+                    if constexpr (thomas_b_last<Num, M>())
                         Num::add(r[i][j], b);
                     else
                         r[i][j] = Num::acc(b);
@@ -289,7 +289,7 @@ PBT_UNROLL
                 give(nm, nrow_, nz);
             }
         };
-        if constexpr (Num::kAddBLast) {
+        if constexpr (thomas_b_last<Num, M>()) {
 PBT_UNROLL
             for (int i = 0; i < M; ++i)
 PBT_UNROLL
