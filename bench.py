@@ -14,13 +14,20 @@ device-resident data with CUDA events on the launching stream; `e2e` times
 the same K solves through the public API with the inputs copied from pinned
 host memory each step and the solution copied back.
 
+The timed method is the chosen one, float-float arithmetic (precision
+"ff"); `plain_fp64` is the same batch with plain FP64 arithmetic, and
+`rel_err_vs_fp64` the chosen result's distance from it.
+
 Extra keys: `roofline` (algorithmic bytes 8*(3m^2+2m) per block row over the
-kernel time, against the measured HBM copy bandwidth), `fp64` (the same
-kernel against the FP64 FMA rate, which is what binds on GB300),
-`cpu_baseline` (the oracle port of the reference CPU path on the host cores,
-on a bounded sample), `variants` (the two-stage P = 16 split of the same
-batch and the long-line case m = 4, nsys = 256, N = 32768, P = 128),
-`clocks` (nvidia-smi sampled during the timed region).
+kernel time, against the measured HBM copy bandwidth; `traffic` = ncu DRAM
+bytes per launch), `plain_fp64` (also against the FP64 FMA rate, which is
+what binds plain FP64 on GB300), `cpu_baseline` (the oracle port of the
+reference CPU path on the host cores, on a bounded sample), `variants` (the
+two-stage P = 16 split of the same batch, the long-line case m = 4,
+nsys = 256, N = 32768, P = 128, and the small case m = 3, nsys = 1024,
+N = 128, P = 4 timed with L2 flushed), `mixed_precision`, `adjoint`,
+`uneven_batch`, `clocks` (nvidia-smi sampled during the timed region).
+`--sections` limits the extra sections (e.g. `--sections main`).
 
 Under torchrun (N > 1) every rank solves its own full batch (weak scaling,
 no collective on the data path); the time is the max over ranks.
@@ -50,7 +57,16 @@ M, NSYS, NROW, NSEG, DELTA, SEED = 5, 65536, 256, 1, 1.2, 20240101
 VARIANTS = [  # name, m, nsys, nrow, nseg, delta
     ("pencil_P16", 5, 65536, 256, 16, 1.2),
     ("long_lines_P128", 4, 256, 32768, 128, 1.2),
+    ("small_P4", 3, 1024, 128, 4, 2.0),  # 34.6 MB: fits in L2, timed with L2 flushed before each solve
 ]
+L2_FIT_BYTES = 256 << 20  # inputs below this are timed with an L2 flush before every solve
+# DRAM bytes (read + write) per block row of k_thomas<FF,5> from ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum on a 65536-system, 32-row
+# batch: 2.349 GB / 2,097,152 rows).  The factor workspace round trip (C'
+# written forward, read back backward) and y make the excess over the
+# algorithmic 680 B; it scales with the rows, so a full launch moves
+# rows * this.
+TRAFFIC_BYTES_PER_ROW = {5: 1120.0}
 # Mixed precision: the pencil batch with every block row scaled by a
 # log-uniform factor in [1e-3, 1e3]; FP32 factorisation + FP64 residual
 # refinement, and float-float, each against the plain FP64 solution.
@@ -330,6 +346,29 @@ def time_device(plan, arrs, dpool, m, nsys, nrow, steps, warmup, ws, dev, solve)
     return ms / 1e3
 
 
+def time_device_flushed(plan, arrs, d0, m, nsys, nrow, steps, warmup, dev, solve):
+    """Like time_device for inputs that fit in L2: before every solve a
+    buffer larger than L2 is overwritten, and only the solve is timed (events
+    around each solve, summed)."""
+    import torch
+
+    a, b, c = arrs
+    scratch = torch.empty(L2_FIT_BYTES // 2, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        solve(plan, a, b, c, d0.clone(), m, nsys, nrow)
+    work = [d0.clone() for _ in range(steps)]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        scratch.fill_(float(i))
+        evs[i][0].record(stream)
+        solve(plan, a, b, c, work[i], m, nsys, nrow)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(e0.elapsed_time(e1) for e0, e1 in evs) / 1e3
+
+
 def rel_err_vs(x, ref, m, nsys, nrow) -> float:
     """max over systems of max|x - ref| / max|ref| (GPU tensors)."""
     X = x.view(m, nrow, nsys)
@@ -426,12 +465,17 @@ def run_ours(args):
         vw, _ = make_workload(vm, vns, vn, vdelta, dev)
         va, vb, vc, vd = (torch.from_numpy(x).to(dev) for x in vw.arrays)
         vrows = vns * vn
-        entry = {"m": vm, "nsys": vns, "nrow": vn, "nseg": vp}
+        entry = {"m": vm, "nsys": vns, "nrow": vn, "nseg": vp,
+                 "l2": "flushed before each solve" if vrows * bytes_per_row(vm) < L2_FIT_BYTES else "inputs > L2"}
         xs = {}
         for prec in ("ff", "fp64"):
             vplan = pbt.BtdmaGpuPlan().create(vm, vns, vn, vp, precision=prec)
             ksteps = max(3, args.steps // 2)
-            vs = time_device(vplan, (va, vb, vc), [vd], vm, vns, vn, ksteps, 3, ws, dev, solve)
+            small = vrows * bytes_per_row(vm) < L2_FIT_BYTES
+            if small:
+                vs = time_device_flushed(vplan, (va, vb, vc), vd, vm, vns, vn, ksteps, 3, dev, solve)
+            else:
+                vs = time_device(vplan, (va, vb, vc), [vd], vm, vns, vn, ksteps, 3, ws, dev, solve)
             vs = max_over_ranks(vs, ws, dev)
             xs[prec] = vd.clone()
             t = pbt.solve_noncyclic_profiled(vplan, va, vb, vc, xs[prec], vm, vns, vn)
@@ -561,7 +605,9 @@ def run_ours(args):
                        "fp64_pipe_frac": rows * fp64_flops_per_row_thomas(m) / kern64_s / (2 * fma["fp64_fma_per_s"])},
         "speedup_vs_plain_fp64": secs64 / secs,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": TRAFFIC_BYTES_PER_ROW[m] * rows if m in TRAFFIC_BYTES_PER_ROW else None,
+                     "traffic_note": "ncu dram bytes per row on a 65536 x 32 batch, scaled to this launch's rows",
                      "peak_source": peaks["source"], "bytes_per_row": bytes_per_row(m),
                      "kernel": f"k_thomas<FF,{m}>"},
         "fma_rates": fma,
