@@ -25,6 +25,12 @@
  * Arrays are device pointers in the reference GPU layout (column-major
  * Fortran A(nsys, nrow, m, m), D(nsys, nrow, m)):
  *   A[sys + nsys*(row + nrow*(i + m*j))],  D[sys + nsys*(row + nrow*i)]
+ * or, for plans created with PBT_FLAG_CPU_LAYOUT, in the layout of the
+ * reference CPU path (Fortran a(m, m, nsys, n), d(m, nsys, n),
+ * Fortran_Original/src/mod_btdma_cpu.f90:18-19):
+ *   A[i + m*(j + m*(sys + nsys*row))],  D[i + m*(sys + nsys*row)]
+ * (such a plan converts on the device through workspace of the size of the
+ * inputs; not with PBT_FLAG_INPLACE or the adjoint).
  * with (i, j) the row and column inside the m x m block
  * (pascal_btdma_cuda.hpp:46-65).  System `sys` solves
  *   A_q x_{q-1} + B_q x_q + C_q x_{q+1} = d_q,   q = 0 .. nrow-1,
@@ -87,6 +93,7 @@ typedef enum pbt_precision {
 #define PBT_FLAG_STAGED_LOADS 0x10u    /* single-segment solve: TMA-staged loads wherever allowed (m <= 6,
                                           nsys >= 32 and even, 16-byte aligned arrays) */
 /* Neither load flag: the library picks per solve (same results either way). */
+#define PBT_FLAG_CPU_LAYOUT 0x20u      /* a, b, c, d are in the reference CPU layout (see below) */
 
 typedef struct pbt_plan_desc {
     int m;                 /* block size, 1..PBT_MAX_BLOCK */

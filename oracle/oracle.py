@@ -84,6 +84,12 @@ def gpu_to_cpu(m, nsys, nrow, is_matrix, g: np.ndarray) -> np.ndarray:
     return out
 
 
+def cpu_to_gpu(m, nsys, nrow, is_matrix, c: np.ndarray) -> np.ndarray:
+    out = np.empty_like(c)
+    lib().pbto_cpu_to_gpu(m, nsys, nrow, int(is_matrix), _p(c), _p(out))
+    return out
+
+
 def dgesv(a: np.ndarray, b: np.ndarray) -> tuple[np.ndarray, int]:
     """dgesv on a column-major (Fortran-ordered) m x m matrix and m x nrhs rhs."""
     a = np.asfortranarray(a, dtype=np.float64).copy(order="F")

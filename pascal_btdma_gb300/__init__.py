@@ -121,6 +121,7 @@ class BtdmaGpuPlan:
     reference_method: bool = False
     direct_loads: bool = False
     staged_loads: bool = False
+    cpu_layout: bool = False
     created: bool = False
     _handle: C.c_void_p = field(default_factory=C.c_void_p, repr=False)
 
@@ -137,6 +138,7 @@ class BtdmaGpuPlan:
         reference_method: bool = False,
         direct_loads: bool = False,
         staged_loads: bool = False,
+        cpu_layout: bool = False,
         tol: float = 1e-12,
         max_iter: int = 8,
         threads_per_block: int = 0,
@@ -154,6 +156,7 @@ class BtdmaGpuPlan:
             | (N.PBT_FLAG_REFERENCE_METHOD if reference_method else 0)
             | (N.PBT_FLAG_DIRECT_LOADS if direct_loads else 0)
             | (N.PBT_FLAG_STAGED_LOADS if staged_loads else 0)
+            | (N.PBT_FLAG_CPU_LAYOUT if cpu_layout else 0)
         )
         d.tol = float(tol)
         d.max_iter = int(max_iter)
@@ -164,7 +167,7 @@ class BtdmaGpuPlan:
         self.m, self.nsys, self.nrow, self.nseg = d.m, d.nsys, d.nrow, d.nseg
         self.precision, self.cyclic, self.inplace = precision, cyclic, inplace
         self.reference_method = reference_method
-        self.direct_loads, self.staged_loads = direct_loads, staged_loads
+        self.direct_loads, self.staged_loads, self.cpu_layout = direct_loads, staged_loads, cpu_layout
         self.created = True
         return self
 
@@ -295,6 +298,17 @@ def matrix_index(sys: int, row: int, p: int, q: int, nsys: int, nrow: int, m: in
 def vector_index(sys: int, row: int, p: int, nsys: int, nrow: int) -> int:
     """Element p of vector (sys, row) (pascal_btdma_cuda.hpp:58-65)."""
     return sys + nsys * (row + nrow * p)
+
+
+def cpu_matrix_index(sys: int, row: int, p: int, q: int, nsys: int, m: int) -> int:
+    """Element (p, q) of block (sys, row) in the reference CPU layout a(m, m, nsys, n)
+    (Fortran_Original/src/mod_btdma_cpu.f90:18), used by plans with cpu_layout=True."""
+    return p + m * (q + m * (sys + nsys * row))
+
+
+def cpu_vector_index(sys: int, row: int, p: int, nsys: int, m: int) -> int:
+    """Element p of vector (sys, row) in the reference CPU layout d(m, nsys, n)."""
+    return p + m * (sys + nsys * row)
 
 
 def adjoint_noncyclic(plan, a, b, c, x, g, da=None, db=None, dc=None, m=None, nsys=None, nrow=None, stream=None) -> None:

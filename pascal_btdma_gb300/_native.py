@@ -31,6 +31,7 @@ PBT_FLAG_INPLACE = 0x2
 PBT_FLAG_REFERENCE_METHOD = 0x4
 PBT_FLAG_DIRECT_LOADS = 0x8
 PBT_FLAG_STAGED_LOADS = 0x10
+PBT_FLAG_CPU_LAYOUT = 0x20
 
 PBT_MAX_BLOCK = 10
 

@@ -56,6 +56,11 @@ struct pbt_plan {
     // residual E, convergence statistic, and the outcome of the last solve.
     double* rx = nullptr;
     double* re_ = nullptr;
+    // PBT_FLAG_CPU_LAYOUT: the inputs in the GPU layout the kernels read.
+    double* la = nullptr;
+    double* lb = nullptr;
+    double* lc = nullptr;
+    double* ld = nullptr;
     // Adjoint of a segmented plan: M^T's blocks, allocated on first use.
     double* at = nullptr;
     double* bt = nullptr;
@@ -307,14 +312,22 @@ int validate(const pbt_plan_desc& d) {
         return fail(PBT_EINVAL, "plan: threads_per_block must be 0 or a multiple of 32 in 32..128");
     }
     const unsigned known = PBT_FLAG_CYCLIC | PBT_FLAG_INPLACE | PBT_FLAG_REFERENCE_METHOD | PBT_FLAG_DIRECT_LOADS |
-                           PBT_FLAG_STAGED_LOADS;
+                           PBT_FLAG_STAGED_LOADS | PBT_FLAG_CPU_LAYOUT;
     if (d.flags & ~known) return fail(PBT_EINVAL, "plan: unknown flag bits");
     if ((d.flags & PBT_FLAG_DIRECT_LOADS) && (d.flags & PBT_FLAG_STAGED_LOADS))
         return fail(PBT_EINVAL, "plan: PBT_FLAG_DIRECT_LOADS and PBT_FLAG_STAGED_LOADS exclude each other");
+    if ((d.flags & PBT_FLAG_CPU_LAYOUT) && (d.flags & PBT_FLAG_INPLACE))
+        return fail(PBT_EUNSUPPORTED, "plan: PBT_FLAG_CPU_LAYOUT works on converted copies, so PBT_FLAG_INPLACE "
+                                      "(factors written into the caller's A and C) is not provided with it");
     return PBT_OK;
 }
 
 void free_plan(pbt_plan* p) {
+    cudaFree(p->la);
+    cudaFree(p->lb);
+    cudaFree(p->lc);
+    cudaFree(p->ld);
+    p->la = p->lb = p->lc = p->ld = nullptr;
     cudaFree(p->at);
     cudaFree(p->bt);
     cudaFree(p->ct);
@@ -440,6 +453,12 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
     return PBT_OK;
 }
 
+int solve_core(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow, bool cyclic,
+               pbt_timings* t, cudaStream_t s);
+
+// Argument checks, then the solve; a PBT_FLAG_CPU_LAYOUT plan converts A, B,
+// C, D into its GPU-layout workspace first and the solution back after
+// (its profiled `total` includes both conversions).
 int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow,
                bool cyclic, pbt_timings* t, void* stream) {
     int rc = check_plan(p);
@@ -458,7 +477,35 @@ int solve_impl(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
     if (!a || !b || !c || !d) return fail(PBT_EINVAL, "solve: null array pointer");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     p->last_stream = s;
+    if (!(ds.flags & PBT_FLAG_CPU_LAYOUT)) return solve_core(p, a, b, c, d, m, nsys, nrow, cyclic, t, s);
 
+    EventSet span(t != nullptr);
+    if (t && !span.ok) return fail(PBT_ECUDA, "solve_profiled: cudaEventCreate failed");
+    cudaError_t e = t ? cudaEventRecord(span.ev[0], s) : cudaSuccess;
+    const int mm = m * m;
+    if (e == cudaSuccess) e = pbt::launch_layout(a, p->la, mm, nsys, nrow, 0, s);
+    if (e == cudaSuccess) e = pbt::launch_layout(b, p->lb, mm, nsys, nrow, 0, s);
+    if (e == cudaSuccess) e = pbt::launch_layout(c, p->lc, mm, nsys, nrow, 0, s);
+    if (e == cudaSuccess) e = pbt::launch_layout(d, p->ld, m, nsys, nrow, 0, s);
+    if (e != cudaSuccess) return cuda_fail(e, "CPU-layout conversion in");
+    rc = solve_core(p, p->la, p->lb, p->lc, p->ld, m, nsys, nrow, cyclic, t, s);
+    if (rc) return rc;
+    if ((e = pbt::launch_layout(p->ld, d, m, nsys, nrow, 1, s)) != cudaSuccess)
+        return cuda_fail(e, "CPU-layout conversion out");
+    if (t) {
+        float tot = 0.f;
+        if ((e = cudaEventRecord(span.ev[1], s)) != cudaSuccess || (e = cudaEventSynchronize(span.ev[1])) != cudaSuccess)
+            return cuda_fail(e, "solve_profiled");
+        cudaEventElapsedTime(&tot, span.ev[0], span.ev[1]);
+        t->total = tot * 1e-3;
+    }
+    return PBT_OK;
+}
+
+int solve_core(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow, bool cyclic,
+               pbt_timings* t, cudaStream_t s) {
+    int rc = PBT_OK;
+    const pbt_plan_desc& ds = p->desc;
     const bool timed = (t != nullptr);
     EventSet evs(timed);
     if (timed && !evs.ok) return fail(PBT_ECUDA, "solve_profiled: cudaEventCreate failed");
@@ -556,6 +603,12 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
         if ((rc = alloc(p, &p->rc, mm * rrows))) goto fail_out;
         if ((rc = alloc(p, &p->rd, (size_t)d.m * rrows))) goto fail_out;
         if (cyclic && (rc = alloc(p, &p->re, mm * rrows))) goto fail_out;
+    }
+    if (d.flags & PBT_FLAG_CPU_LAYOUT) {
+        if ((rc = alloc(p, &p->la, mm * rows))) goto fail_out;
+        if ((rc = alloc(p, &p->lb, mm * rows))) goto fail_out;
+        if ((rc = alloc(p, &p->lc, mm * rows))) goto fail_out;
+        if ((rc = alloc(p, &p->ld, (size_t)d.m * rows))) goto fail_out;
     }
     if (d.precision == PBT_PREC_FP32_REFINE) {
         const size_t nv = (size_t)d.m * rows;
@@ -657,8 +710,9 @@ int pbt_adjoint_noncyclic(pbt_plan* p, const double* a, const double* b, const d
         return fail(PBT_EINVAL, buf);
     }
     if (!a || !b || !c || !x || !g) return fail(PBT_EINVAL, "adjoint: null array pointer");
-    if (ds.flags & (PBT_FLAG_CYCLIC | PBT_FLAG_INPLACE))
-        return fail(PBT_EUNSUPPORTED, "adjoint: needs a non-cyclic plan without PBT_FLAG_INPLACE");
+    if (ds.flags & (PBT_FLAG_CYCLIC | PBT_FLAG_INPLACE | PBT_FLAG_CPU_LAYOUT))
+        return fail(PBT_EUNSUPPORTED,
+                    "adjoint: needs a non-cyclic plan without PBT_FLAG_INPLACE and without PBT_FLAG_CPU_LAYOUT");
     if (ds.precision == PBT_PREC_FP32_REFINE)
         return fail(PBT_EUNSUPPORTED, "adjoint: provided for the fp64 and ff precisions");
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -77,6 +77,10 @@ template <int M> cudaError_t launch_gradients(const SolveArgs& g, const AdjointA
 template <int M> cudaError_t launch_residual(const SolveArgs& g, const double* X, double* E);
 template <int M> cudaError_t launch_accumulate(const SolveArgs& g, double* X, const double* E, unsigned* stat);
 
+// Layout conversion for PBT_FLAG_CPU_LAYOUT plans (pbt_layout.cu): E elements
+// per (system, row); dir 0: CPU layout src -> GPU layout dst, 1: back.
+cudaError_t launch_layout(const double* src, double* dst, int E, int nsys, int nrow, int dir, cudaStream_t s);
+
 // Records the message returned by pbt_last_error_string() on this thread and
 // returns `code` (defined in pbt_api.cpp).
 int set_last_error(int code, const char* msg);

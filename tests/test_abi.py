@@ -104,6 +104,7 @@ def create(**kw):
         (dict(flags=N.PBT_FLAG_CYCLIC), N.PBT_EINVAL, "cyclic"),
         (dict(flags=0x100), N.PBT_EINVAL, "unknown flag"),
         (dict(flags=N.PBT_FLAG_DIRECT_LOADS | N.PBT_FLAG_STAGED_LOADS), N.PBT_EINVAL, "exclude each other"),
+        (dict(flags=N.PBT_FLAG_CPU_LAYOUT | N.PBT_FLAG_INPLACE), N.PBT_EUNSUPPORTED, "CPU_LAYOUT"),
         (dict(threads_per_block=48), N.PBT_EINVAL, "threads_per_block"),
         (dict(precision=7), N.PBT_EUNSUPPORTED, "precision"),
         (dict(precision=N.PBT_PREC_FP32_REFINE, flags=N.PBT_FLAG_INPLACE), N.PBT_EINVAL, "unchanged"),
@@ -152,3 +153,20 @@ def test_python_mirror_errors():
 def test_index_helpers_match_reference_layout():
     assert pbt.matrix_index(1, 2, 0, 1, 4, 5, 3) == 1 + 4 * (2 + 5 * (0 + 3 * 1))
     assert pbt.vector_index(3, 4, 2, 8, 6) == 3 + 8 * (4 + 6 * 2)
+
+
+def test_cpu_layout_index_helpers_match_oracle_conversion():
+    """pbt.cpu_matrix_index / cpu_vector_index agree with the oracle's layout
+    conversion (the reference CPU layout a(m, m, nsys, n), d(m, nsys, n))."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    m, nsys, nrow = 3, 5, 4
+    g = np.arange(m * m * nsys * nrow, dtype=np.float64)
+    c = O.gpu_to_cpu(m, nsys, nrow, True, g)
+    gv = np.arange(m * nsys * nrow, dtype=np.float64)
+    cv = O.gpu_to_cpu(m, nsys, nrow, False, gv)
+    for sys, row, p, q in [(0, 0, 0, 0), (4, 3, 2, 1), (2, 1, 1, 2)]:
+        assert c[pbt.cpu_matrix_index(sys, row, p, q, nsys, m)] == g[pbt.matrix_index(sys, row, p, q, nsys, nrow, m)]
+        assert cv[pbt.cpu_vector_index(sys, row, p, nsys, m)] == gv[pbt.vector_index(sys, row, p, nsys, nrow)]

@@ -122,3 +122,56 @@ def test_adjoint_rejects_inplace_and_bad_sizes(cuda):
         plan.create(3, 32, 12, 1)
         with pytest.raises(ValueError, match="do not match"):
             pbt.adjoint_noncyclic(plan, a, b, c, d, d.clone(), m=3, nsys=32, nrow=13)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_adjoint_full_size_finite_differences(cuda, prec):
+    """The adjoint workload at its full size: m = 4, nsys = 16384, N = 512,
+    P = 8, delta = 1.5, L = sum(w . x) with w iid U[-1, 1).  dL/dA, dL/dB,
+    dL/dC, dL/dd from the adjoint kernel against central differences
+    (h = 1e-6, FP64 solves) on 64 random entries of each; entries are
+    perturbed in place and restored.  The system index is fastest in the
+    layout, so entry e belongs to system e % nsys."""
+    m, nsys, nrow, nseg = 4, 16384, 512, 8
+    wl = synth.dominant(m, nsys, nrow, seed=5, delta=1.5)
+    dev = torch.device(cuda)
+    A, B, C, d = (torch.from_numpy(t).to(dev) for t in wl.arrays)
+    wts = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, nsys * nrow * m)).to(dev)
+    with pbt.BtdmaGpuPlan() as plan, pbt.BtdmaGpuPlan() as plan64:
+        plan.create(m, nsys, nrow, nseg, precision=prec)
+        plan64.create(m, nsys, nrow, nseg, precision="fp64")
+        x = d.clone()
+        pbt.solve_noncyclic(plan, A, B, C, x, m, nsys, nrow)
+        lam = wts.clone()
+        dA, dB, dC = torch.empty_like(A), torch.empty_like(B), torch.empty_like(C)
+        pbt.adjoint_noncyclic(plan, A, B, C, x, lam, dA, dB, dC)
+        assert plan.status() == 0
+        xx = torch.empty_like(d)
+        w2 = wts.view(-1, nsys)
+
+        def L(sys):
+            # An entry of system `sys` moves only that system's x, so L's
+            # change is that system's share of the sum: summing only it
+            # keeps the rounding of the other 16383 systems out of the
+            # difference quotient.
+            xx.copy_(d)
+            pbt.solve_noncyclic(plan64, A, B, C, xx, m, nsys, nrow)
+            return float(torch.dot(w2[:, sys], xx.view(-1, nsys)[:, sys]))
+
+        rng = np.random.default_rng(4)
+        h = 1e-6
+        for arr, grad in ((A, dA), (B, dB), (C, dC), (d, lam)):
+            flat = arr.view(-1)
+            idx = rng.choice(flat.numel(), size=64, replace=False)
+            fd = np.empty(64)
+            for k, e in enumerate(idx.tolist()):
+                v = float(flat[e])
+                flat[e] = v + h
+                lp = L(e % nsys)
+                flat[e] = v - h
+                lm = L(e % nsys)
+                flat[e] = v
+                fd[k] = (lp - lm) / (2 * h)
+            an = grad.view(-1)[torch.from_numpy(idx).to(dev)].cpu().numpy()
+            err = np.abs(fd - an).max()
+            assert err <= 1e-6 * max(1.0, np.abs(an).max()), err
