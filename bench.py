@@ -79,6 +79,15 @@ ADJ = dict(m=4, nsys=16384, nrow=512, delta=1.5, segs=(8, 1), pressure_tiles=16)
 # {2, 3, 4, 5}, delta = 1.5; one persistent launch per sweep, 100 sweeps in a
 # CUDA graph; tuning by the autotuner; against one plain launch per (m, N).
 UNEVEN = dict(nsys=32768, nmin=16, nmax=4096, mmin=2, mmax=5, delta=1.5, sweeps=100)
+METRIC = "block-rows/s (chosen method at <=1e-10 rel err vs plain FP64)"
+DATA = "synthetic (seeded Philox4x32-10, diagonally dominant, delta=1.2)"
+
+
+def workload_config(ws: int) -> dict:
+    """The `config` of both arms' JSON lines (the same workload)."""
+    return {"workload": f"pencil batch m={M}, nsys={NSYS}, N={NROW}, P={NSEG}", "m": M, "nsys": NSYS,
+            "nrow": NROW, "nseg": NSEG, "l2": "inputs 11.4 GB > L2 (no flush needed)",
+            "parallelism": f"replicas x{ws}"}
 
 
 def run_uneven(dev, log=None) -> dict:
@@ -428,32 +437,48 @@ def run_ours(args):
     achieved = rows * bytes_per_row(m) / kern_s / 1e9
     achieved64 = rows * bytes_per_row(m) / kern64_s / 1e9
 
-    # End to end through the public API: pinned H2D of A, B, C, D, solve, D2H of x.
-    out_h = torch.empty_like(hD).pin_memory()
+    # End to end through the public API: every step copies its A, B, C, D from
+    # pinned host memory, solves, and copies x back.  As a caller streaming
+    # batches would, two plans and two device buffer sets alternate on two
+    # streams, so one step's solve and D2H overlap the next step's H2D (the
+    # host link, ~211 GB/s H2D on this system, is the bound).
+    out_h = [torch.empty_like(hD).pin_memory() for _ in range(2)]
+    dev_sets = [(a, b, c, d0)] + [tuple(torch.empty_like(t) for t in (a, b, c, d0))]
+    e2e_plans = [plans["ff"], pbt.BtdmaGpuPlan().create(m, nsys, nrow, nseg, precision="ff")]
+    e2e_streams = [torch.cuda.Stream(), torch.cuda.Stream()]
 
-    def e2e_step():
-        a.copy_(hA, non_blocking=True)
-        b.copy_(hB, non_blocking=True)
-        c.copy_(hC, non_blocking=True)
-        d0.copy_(hD, non_blocking=True)
-        solve(plans["ff"], a, b, c, d0, m, nsys, nrow)
-        out_h.copy_(d0, non_blocking=True)
+    def e2e_step(i):
+        k = i % 2
+        sa, sb, sc, sd = dev_sets[k]
+        with torch.cuda.stream(e2e_streams[k]):
+            sa.copy_(hA, non_blocking=True)
+            sb.copy_(hB, non_blocking=True)
+            sc.copy_(hC, non_blocking=True)
+            sd.copy_(hD, non_blocking=True)
+            solve(e2e_plans[k], sa, sb, sc, sd, m, nsys, nrow, stream=e2e_streams[k])
+            out_h[k].copy_(sd, non_blocking=True)
 
-    for _ in range(2):
-        e2e_step()
+    st = torch.cuda.current_stream()
+    for i in range(2):
+        e2e_step(i)
     torch.cuda.synchronize()
     barrier(ws)
-    st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
-    for _ in range(args.steps):
-        e2e_step()
+    for s_ in e2e_streams:
+        s_.wait_event(e0)
+    for i in range(args.steps):
+        e2e_step(i)
+    for s_ in e2e_streams:
+        st.wait_stream(s_)
     e1.record(st)
     torch.cuda.synchronize()
     barrier(ws)
     e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws, dev)
     h2d = 3 * hA.numel() * 8 + hD.numel() * 8
     d2h = hD.numel() * 8
+    e2e_plans[1].destroy()
+    del dev_sets, e2e_streams
 
     # Variants: the two-stage split and the long lines, both arithmetics.
     variants = {}
@@ -581,7 +606,7 @@ def run_ours(args):
     uneven = run_uneven(dev) if "uneven" in args.sections else {}
 
     result = {
-        "metric": "block-rows/s (chosen method at <=1e-10 rel err vs plain FP64)",
+        "metric": METRIC,
         "value": value,
         "unit": "block-rows/s",
         "n_gpus": ws,
@@ -592,11 +617,9 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64 data, float-float (2 x f32) arithmetic",
-        "data": "synthetic (seeded Philox4x32-10, diagonally dominant, delta=1.2)",
-        "config": {"workload": f"pencil batch m={m}, nsys={nsys}, N={nrow}, P={nseg}", "m": m,
-                   "nsys": nsys, "nrow": nrow, "nseg": nseg,
-                   "method": "block Thomas, pivoted LU, float-float arithmetic (precision='ff')",
-                   "l2": "inputs 11.4 GB > L2 (no flush needed)", "parallelism": f"replicas x{ws}"},
+        "data": DATA,
+        "config": workload_config(ws),
+        "method": "block Thomas, pivoted LU, float-float arithmetic (precision='ff')",
         "rel_err_vs_fp64": rel_err,
         "fp64_backward_err": backward_err,
         "plain_fp64": {"value": ws * rows * args.steps / secs64, "ms_per_step": kern64_s * 1e3,
@@ -612,7 +635,9 @@ def run_ours(args):
                      "kernel": f"k_thomas<FF,{m}>"},
         "fma_rates": fma,
         "e2e": {"value": ws * rows * args.steps / e2e_s, "unit": "block-rows/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_s / args.steps * 1e3,
+                "pipelining": "2 streams, 2 plans, 2 device buffer sets; step i+1's H2D overlaps step i's solve + D2H"},
         "gpu_launches": args.steps,
         "clocks": clocks,
         "variants": variants,
@@ -640,7 +665,7 @@ def run_reference(args):
 
     threads = O.default_threads()
     m, nrow, nseg = M, NROW, NSEG
-    nsys_s = 4096
+    nsys_s = 16384
     w = synth.dominant(m, nsys_s, nrow, seed=SEED, delta=DELTA)
     cpu = [O.gpu_to_cpu(m, nsys_s, nrow, k < 3, x) for k, x in enumerate(w.arrays)]
     times = []
@@ -658,12 +683,12 @@ def run_reference(args):
               f"mod_btdma_cpu on {threads} threads")
     print(json.dumps({
         "impl": "reference",
-        "metric": "block-rows/s (chosen method at <=1e-10 rel err; plain FP64)",
+        "metric": METRIC,
         "value": value, "unit": "block-rows/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox4x32-10, delta=1.2)",
-        "config": {"workload": f"pencil batch m={m}, nsys={NSYS}, N={nrow}, P={nseg}, FP64", "m": m,
-                   "nsys": NSYS, "nrow": nrow, "nseg": nseg},
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": workload_config(ws),
+        "method": "the reference's CPU path (oracle C port of mod_btdma_cpu: block Thomas, LAPACK-style dgesv), FP64",
         "cpu_baseline": {"value": value, "unit": "block-rows/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "block-rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
