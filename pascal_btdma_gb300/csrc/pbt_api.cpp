@@ -236,13 +236,22 @@ bool encode_columns(CUtensorMap* tm, const double* base, int nsys, int nrow, int
 
 // Launch the single-segment block Thomas solve, with TMA-staged loads
 // (k_thomas_staged) or direct loads (k_thomas); both give the same bits.
-// Staging wins where too few warps are resident to hide the loads' latency
-// -- batches of under 8 warps (256 systems) per SM -- and for the FP32
-// factorisation, which is bound by memory rather than arithmetic; with more
-// warps the direct kernel is a few percent faster (GB300, m = 5: float-float
-// 7.1 vs 7.2 ms on 65536 systems, 4.8 vs 7.2 ms staged on 16384).  The plan
+// The default follows GB300 measurements (float-float unless noted, N = 256
+// or 512): staged loads win for the FP32 factorisation of the refined solve,
+// which is bound by memory (m = 5, 65536 systems: 11.5 vs 12.2 ms); for
+// float-float only at m = 4 (16384 systems: 4.48 vs 5.54 ms) -- elsewhere
+// the direct kernel with rolled column loops is faster even on small batches
+// (m = 5, 16384 systems: 4.37 vs 6.02 ms); for FP64 at m = 5, 6 on batches
+// under 8 warps per SM (m = 5, 16384 systems: 4.98 vs 5.24 ms).  The plan
 // flags force either; staging also needs m <= 6, nsys >= 32, nsys even and
 // 16-byte aligned arrays (the tensor-map rules), else direct loads run.
+bool prefer_staged(int arith, int m, int nsys, int sms) {
+    const bool small = sms <= 0 || (nsys + 31) / 32 < 8 * sms;
+    if (arith == kF32) return true;
+    if (arith == kFF) return m == 4 && small;
+    return (m == 5 || m == 6) && small;
+}
+
 cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveArgs& g) {
     const pbt_plan_desc& ds = p->desc;
     bool staged;
@@ -251,7 +260,7 @@ cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveA
     else if (ds.flags & PBT_FLAG_STAGED_LOADS)
         staged = true;
     else
-        staged = arith == kF32 || p->sms <= 0 || (g.nsys + 31) / 32 < 8 * p->sms;
+        staged = prefer_staged(arith, m, g.nsys, p->sms);
     if (staged && m <= pbt::kStagedMaxBlock && g.nsys >= 32) {
         pbt::ThomasMaps maps;
         const int mm = m * m;

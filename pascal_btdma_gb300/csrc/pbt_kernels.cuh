@@ -434,13 +434,26 @@ PBT_UNROLL
 #endif
 // Load scheduling of thomas_body_lu, chosen per block size by measurement
 // (GB300, float-float, 65536 systems): prefetching the next C column one
-// column ahead helps m = 5 (7.09 -> 6.91 ms, N = 256); reading A and C
+// column ahead helps m = 5 (7.09 -> 6.91 ms, N = 256; FP64 neither gains nor
+// has the registers for it); reading A and C
 // through the read-only path, which lets the assembler move C loads past the
 // factor stores, helps m = 6 (10.38 -> 9.27 ms, N = 128); together they lose
 // (registers).
-template <int M>
+// Loops over block columns kept rolled (one copy of the column's code
+// instead of m): the fully unrolled float-float row is ~100 KB of code, and
+// with a dozen warps at different points of it the warps stall on
+// instruction fetch.  Measured on GB300 (65536 systems, float-float): m = 5
+// 6.89 -> 6.53 ms, m = 6 9.02 -> 6.00 ms with both the C-column and the
+// A-column loops rolled; FP64 (smaller code, bound by its pipe) gains
+// nothing and keeps them unrolled.  A rolled A loop reads y_{q-1}[k] from
+// shared memory (cps slot M*M + k) instead of a register.
+template <class Num>
+__host__ __device__ constexpr bool lu_rolled() {
+    return Num::kConv;
+}
+template <class Num, int M>
 __host__ __device__ constexpr bool lu_prefetch_c() {
-    return M == 5;
+    return M == 5 && Num::kConv;
 }
 template <int M>
 __host__ __device__ constexpr bool lu_ldg() {
@@ -463,7 +476,8 @@ __host__ __device__ constexpr bool thomas_b_last() {
 // Block Thomas with the row step split into factor and column solves
 // (lu_factor / lu_solve), for the register-resident block sizes.  The
 // previous row's C' lives in shared memory (`cps`: this thread's M*M raw
-// values, element (k, j) at cps[(k*M + j) * cstride]) instead of registers:
+// values, element (k, j) at cps[(k*M + j) * cstride], then y_{q-1} at
+// cps[(M*M + k) * cstride]) instead of registers:
 // the row reads it one row k at a time, so the registers hold the row's
 // accumulators, the factors and one column, not also C'_{q-1} and every
 // right-hand side.  With thomas_b_last, R_q = -A_q C'_{q-1} + B_q is
@@ -518,17 +532,22 @@ PBT_UNROLL
         if (q > 0) {
             const size_t plane = opaque(plane0);
             const double* pa = A + o;
-PBT_UNROLL
+#pragma unroll(lu_rolled<Num>() ? 1 : M)
             for (int k = 0; k < M; ++k) {
                 T ck[M];
 PBT_UNROLL
                 for (int j = 0; j < M; ++j) ck[j] = Num::lds(cps + (k * M + j) * cstride);
+                T yk;
+                if constexpr (lu_rolled<Num>())
+                    yk = Num::lds(cps + (M * M + k) * cstride);
+                else
+                    yk = y[k];
 PBT_UNROLL
                 for (int i = 0; i < M; ++i, pa += plane) {
                     const T a = lu_ldg<M>() ? Num::in_ro(pa) : Num::in(pa);
 PBT_UNROLL
                     for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
-                    Num::msub(xd[i], a, y[k]);
+                    Num::msub(xd[i], a, yk);
                 }
                 if (PBT_ROW_FENCE) mem_fence_compiler();
             }
@@ -537,6 +556,10 @@ PBT_UNROLL
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
         lu_solve<Num, M>(lu, xd, y);
+        if constexpr (lu_rolled<Num>()) {
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::sts(cps + (M * M + k) * cstride, y[k]);
+        }
         {
             const size_t plane = opaque(plane0);
             if (last) {
@@ -555,15 +578,15 @@ PBT_UNROLL
         // flight whatever the aliasing (lu_prefetch_c, lu_ldg).
         auto ld_c = [&](const double* p) -> double { return (lu_ldg<M>() && raw) ? __ldg(p) : *p; };
         double nxt[M];
-        if constexpr (lu_prefetch_c<M>()) {
+        if constexpr (lu_prefetch_c<Num, M>()) {
 PBT_UNROLL
             for (int i = 0; i < M; ++i, pc += plane) nxt[i] = ld_c(pc);
         }
-PBT_UNROLL
+#pragma unroll(lu_rolled<Num>() ? 1 : M)
         for (int j = 0; j < M; ++j) {
             Acc cj[M];
             T xj[M];
-            if constexpr (lu_prefetch_c<M>()) {
+            if constexpr (lu_prefetch_c<Num, M>()) {
                 double cur[M];
 PBT_UNROLL
                 for (int i = 0; i < M; ++i) cur[i] = nxt[i];
@@ -1420,7 +1443,7 @@ inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) /
 template <class Num, int M>
 cudaError_t launch_thomas(const SolveArgs& g) {
     const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
-    const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * M * M * sizeof(double) : 0;
+    const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * (M * M + M) * sizeof(double) : 0;
     k_thomas<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g);
     return cudaGetLastError();
 }

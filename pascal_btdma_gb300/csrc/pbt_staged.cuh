@@ -96,21 +96,35 @@ __device__ __forceinline__ void fence_proxy_async_shared() {
 }
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
-// Shared memory of one CTA: the ring (R items of M*32 doubles) and C'_{q-1}
-// (M*M*32 raw values).  Sized so that 15 one-warp CTAs fit in an SM
-// (15 * (14 KB + 1 KB reserved) <= 228 KB): 15 * 152 = 2280 resident warps
-// cover a 65536-system batch (2048 warps) in one wave.
-constexpr int kStagedSmemBudget = 14336;
-template <int M>
-__host__ __device__ constexpr int staged_ring() {
-    return (kStagedSmemBudget - M * M * 256) / (M * 256 + 8) < 4 ? 4
-           : (kStagedSmemBudget - M * M * 256) / (M * 256 + 8) > 3 * (1 + 3 * M)
-               ? 3 * (1 + 3 * M)
-               : (kStagedSmemBudget - M * M * 256) / (M * 256 + 8);
+// Block-column loops kept rolled (see lu_rolled) only where that measured
+// faster in this kernel, float-float and FP32 at m = 4 (GB300, 16384
+// systems: 4.48 vs 4.67 ms; 131072: 14.7 vs 15.9 ms); at m = 3, 5, 6 the
+// runtime item bookkeeping of a rolled loop costs more than the smaller
+// code saves.
+template <class Num, int M>
+__host__ __device__ constexpr bool staged_rolled() {
+    return lu_rolled<Num>() && M == 4;
 }
-template <int M>
+// Shared memory of one CTA: the ring (R items of M*32 doubles), C'_{q-1}
+// (M*M*32 raw values) and, with rolled loops, y_{q-1} (M*32).  Sized so that
+// 14 one-warp CTAs fit in an SM (14 * (15.06 KB + 1 KB reserved) <= 228 KB):
+// 14 * 152 = 2128 resident warps cover a 65536-system batch (2048 warps) in
+// one wave, with a 6-item ring at m = 5.
+constexpr int kStagedSmemBudget = 15424;
+template <class Num, int M>
+__host__ __device__ constexpr int staged_fixed_slots() {
+    return M * M + (staged_rolled<Num, M>() ? M : 0);
+}
+template <class Num, int M>
+__host__ __device__ constexpr int staged_ring() {
+    return (kStagedSmemBudget - staged_fixed_slots<Num, M>() * 256) / (M * 256 + 8) < 4 ? 4
+           : (kStagedSmemBudget - staged_fixed_slots<Num, M>() * 256) / (M * 256 + 8) > 3 * (1 + 3 * M)
+               ? 3 * (1 + 3 * M)
+               : (kStagedSmemBudget - staged_fixed_slots<Num, M>() * 256) / (M * 256 + 8);
+}
+template <class Num, int M>
 __host__ __device__ constexpr int staged_smem_bytes() {
-    return (staged_ring<M>() * M + M * M) * 32 * 8;
+    return (staged_ring<Num, M>() * M + staged_fixed_slots<Num, M>()) * 32 * 8;
 }
 
 // Forward item k of a row: which array and which plane offset.  Items:
@@ -163,7 +177,7 @@ template <class Num, int M>
 __global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const __grid_constant__ ThomasMaps maps, const SolveArgs g) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
-    constexpr int R = staged_ring<M>();
+    constexpr int R = staged_ring<Num, M>();
     constexpr int K = 1 + 3 * M;  // forward items per row
     constexpr int K2 = M + 1;     // backward items per row
     constexpr unsigned kSlotBytes = M * 32 * 8;
@@ -239,7 +253,8 @@ __global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const
 
     bool bad = false;
     T y[M];
-    double* const cps = ring + R * M * 32 + lane;  // this lane's C'_{q-1}: (k, j) at cps[32 * (k*M + j)]
+    // This lane's C'_{q-1}: (k, j) at cps[32 * (k*M + j)]; y_{q-1}[k] at cps[32 * (M*M + k)].
+    double* const cps = ring + R * M * 32 + lane;
     for (int q = 0; q < N; ++q) {
         const size_t o = (size_t)q * g.nsys;
         const bool last = (q == N - 1);
@@ -254,19 +269,24 @@ PBT_UNROLL
         }
         // Items 1..2M: the A and B columns in the order fwd_item gives.
         auto a_cols = [&](int k0) {
-PBT_UNROLL
+#pragma unroll(staged_rolled<Num, M>() ? 1 : M)
             for (int k = 0; k < M; ++k) {
                 const double* p = take();
                 if (q > 0) {
                     T ck[M];
 PBT_UNROLL
                     for (int j = 0; j < M; ++j) ck[j] = Num::lds(cps + 32 * (k * M + j));
+                    T yk;
+                    if constexpr (staged_rolled<Num, M>())
+                        yk = Num::lds(cps + 32 * (M * M + k));
+                    else
+                        yk = y[k];
 PBT_UNROLL
                     for (int i = 0; i < M; ++i) {
                         const T a = Num::in(p + 32 * i);
 PBT_UNROLL
                         for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
-                        Num::msub(xd[i], a, y[k]);
+                        Num::msub(xd[i], a, yk);
                     }
                 }
                 const CUtensorMap* nm = fwd_next(q, k0 + k, nrow_, nz);
@@ -303,6 +323,10 @@ PBT_UNROLL
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
         lu_solve<Num, M>(lu, xd, y);
+        if constexpr (staged_rolled<Num, M>()) {
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::sts(cps + 32 * (M * M + k), y[k]);
+        }
         {
             const size_t plane = opaque(plane0);
             if (!last) {
@@ -313,7 +337,7 @@ PBT_UNROLL
         }
         const size_t plane = opaque(plane0);
         double* pw = CW + o;
-PBT_UNROLL
+#pragma unroll(staged_rolled<Num, M>() ? 1 : M)
         for (int j = 0; j < M; ++j) {
             const double* p = take();
             if (!last) {
@@ -413,7 +437,7 @@ PBT_UNROLL
 template <class Num, int M>
 cudaError_t launch_thomas_staged(const SolveArgs& g, const ThomasMaps& maps) {
     if (M > kStagedMaxBlock) return cudaErrorNotSupported;
-    constexpr int smem = staged_smem_bytes<M>();
+    constexpr int smem = staged_smem_bytes<Num, M>();
     static bool configured = false;  // per instantiation; idempotent, so a race is harmless
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(k_thomas_staged<Num, M>,
