@@ -32,6 +32,19 @@ __device__ __forceinline__ int warp_claim(int* head) {
     return __shfl_sync(0xffffffffu, v, 0);
 }
 
+// The single-segment items of the float-float (and FP32) batch run the split
+// form with rolled column loops (thomas_body_lu): one kernel holds the code
+// of every block size, so code size matters even more than in k_thomas.
+#ifndef PBT_BATCH_LU
+#define PBT_BATCH_LU 1
+#endif
+template <class Num>
+__host__ __device__ constexpr bool batch_uses_lu() {
+    return PBT_BATCH_LU && Num::kConv;
+}
+// Shared memory a lane needs for thomas_body_lu at the largest batch block size.
+constexpr int kBatchLuSlots = 5 * 5 + 5;
+
 template <class Num, int M>
 __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTile& tl, int t, int seg, bool& bad) {
     const int lane = threadIdx.x & 31;
@@ -40,8 +53,16 @@ __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTil
     const bool active = lane < tl.lanes && n_lane >= 2;
     const size_t mo = (size_t)tl.mat_off + lane, vo = (size_t)tl.vec_off + lane;
     if (seg < 0) {
-        if (active)
-            thomas_body<Num, M>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo, plane, rs, n_lane, true, bad);
+        if (active) {
+            if constexpr (batch_uses_lu<Num>()) {
+                extern __shared__ double batch_cps[];
+                thomas_body_lu<Num, M>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo,
+                                       batch_cps + threadIdx.x, blockDim.x, plane, rs, n_lane, true, bad);
+            } else {
+                thomas_body<Num, M>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo, plane, rs, n_lane, true,
+                                    bad);
+            }
+        }
         return;
     }
     const size_t rplane = (size_t)32 * 2 * tl.nseg;
@@ -197,11 +218,12 @@ cudaError_t launch_batch(const BatchArgs& ba, int warps, cudaStream_t s, int* gr
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<Num>, 32 * warps, 0);
+    const size_t smem = batch_uses_lu<Num>() ? (size_t)32 * warps * kBatchLuSlots * sizeof(double) : 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<Num>, 32 * warps, smem);
     if (e != cudaSuccess) return e;
     const int grid = sms * (per_sm > 0 ? per_sm : 1);
     if (grid_out) *grid_out = grid;
-    k_batch<Num><<<grid, 32 * warps, 0, s>>>(ba);
+    k_batch<Num><<<grid, 32 * warps, smem, s>>>(ba);
     return cudaGetLastError();
 }
 
