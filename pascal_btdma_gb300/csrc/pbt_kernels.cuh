@@ -455,6 +455,13 @@ template <class Num, int M>
 __host__ __device__ constexpr bool lu_prefetch_c() {
     return M == 5 && Num::kConv;
 }
+// Same for the columns of A at m = 5 (float-float, 65536 systems: 6.15 ->
+// 6.14 ms; 16384 systems: 3.81 -> 3.15 ms); at m = 6 it costs registers
+// (5.83 -> 6.23 ms).
+template <class Num, int M>
+__host__ __device__ constexpr bool lu_prefetch_a() {
+    return M == 5 && Num::kConv;
+}
 template <int M>
 __host__ __device__ constexpr bool lu_ldg() {
     return M == 6;
@@ -465,14 +472,6 @@ template <int M>
 __host__ __device__ constexpr bool thomas_uses_lu() {
     return M >= kThomasLuMinBlock && M <= kThomasLuMaxBlock;
 }
-// Whether a row accumulates R = -A C'_{q-1} from zero and adds B last
-// (Num::kAddBLast) -- only in the split form; the fused form starts from B.
-// The staged kernel follows the same rule, so both give the same bits.
-template <class Num, int M>
-__host__ __device__ constexpr bool thomas_b_last() {
-    return Num::kAddBLast && thomas_uses_lu<M>();
-}
-
 // Block Thomas with the row step split into factor and column solves
 // (lu_factor / lu_solve), for the register-resident block sizes.  The
 // previous row's C' lives in shared memory (`cps`: this thread's M*M raw
@@ -480,10 +479,11 @@ __host__ __device__ constexpr bool thomas_b_last() {
 // cps[(M*M + k) * cstride]) instead of registers:
 // the row reads it one row k at a time, so the registers hold the row's
 // accumulators, the factors and one column, not also C'_{q-1} and every
-// right-hand side.  With thomas_b_last, R_q = -A_q C'_{q-1} + B_q is
-// accumulated from zero with B added last; otherwise from B, as thomas_body.
-// The operations and their order are exactly those of the TMA-staged kernel
-// k_thomas_staged, so the two agree bit for bit.
+// right-hand side.  R_q = B_q - A_q C'_{q-1} starts from B, as in
+// thomas_body (adding B last instead measured slower in this form, and costs
+// m*m extra FP64 adds in the FP64 solve).  The operations and their order are
+// exactly those of the TMA-staged kernel k_thomas_staged, so the two agree
+// bit for bit.
 template <class Num, int M>
 __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B, const double* C, double* D,
                                                double* CW, double* cps, int cstride, size_t plane0, size_t rs,
@@ -505,33 +505,24 @@ __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B,
 PBT_UNROLL
             for (int i = 0; i < M; ++i, pd += plane) xd[i] = Num::acc(Num::in(pd));
         }
-        // R = B - A C'_{q-1}: from B (thomas_b_last false) or from zero with
-        // B added last, in the order the staged kernel receives the blocks.
-        auto add_b = [&]() {
+        {
             const size_t plane = opaque(plane0);
             const double* pb = B + o;
 PBT_UNROLL
             for (int j = 0; j < M; ++j)
 PBT_UNROLL
-                for (int i = 0; i < M; ++i, pb += plane) {
-                    const T b = Num::in_ro(pb);
-                    if constexpr (thomas_b_last<Num, M>())
-                        Num::add(r[i][j], b);
-                    else
-                        r[i][j] = Num::acc(b);
-                }
-        };
-        if constexpr (thomas_b_last<Num, M>()) {
-PBT_UNROLL
-            for (int i = 0; i < M; ++i)
-PBT_UNROLL
-                for (int j = 0; j < M; ++j) r[i][j] = Num::acc0();
-        } else {
-            add_b();
+                for (int i = 0; i < M; ++i, pb += plane) r[i][j] = Num::acc(Num::in_ro(pb));
         }
         if (q > 0) {
             const size_t plane = opaque(plane0);
             const double* pa = A + o;
+            // lu_prefetch_a: column k+1 of A is loaded (raw) before column k is
+            // used, so one column is always in flight.
+            double an[M];
+            if constexpr (lu_prefetch_a<Num, M>()) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) an[i] = __ldg(pa);
+            }
 #pragma unroll(lu_rolled<Num>() ? 1 : M)
             for (int k = 0; k < M; ++k) {
                 T ck[M];
@@ -542,9 +533,24 @@ PBT_UNROLL
                     yk = Num::lds(cps + (M * M + k) * cstride);
                 else
                     yk = y[k];
+                double ac[M];
+                if constexpr (lu_prefetch_a<Num, M>()) {
 PBT_UNROLL
-                for (int i = 0; i < M; ++i, pa += plane) {
-                    const T a = lu_ldg<M>() ? Num::in_ro(pa) : Num::in(pa);
+                    for (int i = 0; i < M; ++i) ac[i] = an[i];
+                    if (k + 1 < M) {
+PBT_UNROLL
+                        for (int i = 0; i < M; ++i, pa += plane) an[i] = __ldg(pa);
+                    }
+                }
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) {
+                    T a;
+                    if constexpr (lu_prefetch_a<Num, M>()) {
+                        a = Num::in(&ac[i]);
+                    } else {
+                        a = lu_ldg<M>() ? Num::in_ro(pa) : Num::in(pa);
+                        pa += plane;
+                    }
 PBT_UNROLL
                     for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
                     Num::msub(xd[i], a, yk);
@@ -552,7 +558,6 @@ PBT_UNROLL
                 if (PBT_ROW_FENCE) mem_fence_compiler();
             }
         }
-        if constexpr (thomas_b_last<Num, M>()) add_b();
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
         lu_solve<Num, M>(lu, xd, y);

@@ -17,8 +17,7 @@
 //   in(p)        load an FP64 input element and convert to T
 //   out(p, v)    convert T to FP64 and store
 //   lds/sts      raw 8-byte workspace slots (no conversion)
-//   acc(x), mac(acc, x, y) (acc += x*y), msub(acc, x, y) (acc -= x*y),
-//   add(acc, x) (acc += x), fin(acc)
+//   acc(x), mac(acc, x, y) (acc += x*y), msub(acc, x, y) (acc -= x*y), fin(acc)
 //   mul, rcp, neg, zero, one, key (|x| as an ordered integer), sel, is_zero
 //
 // FP64 <-> FF conversion uses integer bit operations only, so the FF path
@@ -52,10 +51,6 @@ struct F64 {
         double v;
     };
     static constexpr bool kConv = false;  // raw workspace values differ from FP64?
-    // Block Thomas row: R = B - A C' starts from B (false) or accumulates
-    // -A C' from zero and adds B last (true).  Adding B last costs m*m adds,
-    // which on the FP64 pipe (the bound of the F64 solve) is ~7% of a row.
-    static constexpr bool kAddBLast = false;
 
     __device__ static __forceinline__ T in(const double* p) { return *p; }
     __device__ static __forceinline__ T in_ro(const double* p) { return __ldg(p); }
@@ -67,7 +62,6 @@ struct F64 {
     __device__ static __forceinline__ Acc acc0() { return {0.0}; }
     __device__ static __forceinline__ void mac(Acc& a, T x, T y) { a.v = fma(x, y, a.v); }
     __device__ static __forceinline__ void msub(Acc& a, T x, T y) { a.v = fma(-x, y, a.v); }
-    __device__ static __forceinline__ void add(Acc& a, T x) { a.v = __dadd_rn(a.v, x); }
     __device__ static __forceinline__ T fin(Acc a) { return a.v; }
 
     __device__ static __forceinline__ T mul(T a, T b) { return a * b; }
@@ -107,7 +101,6 @@ struct FF {
         float s, t;  // unnormalised: value = s + t, t collects rounding errors and low parts
     };
     static constexpr bool kConv = true;
-    static constexpr bool kAddBLast = true;
 
     // FP64 -> (h, l) by bit manipulation: h = x truncated to 24 significant
     // bits, l = the next 23 bits.  |x - (h + l)| < 2^-46 |x| for
@@ -161,12 +154,6 @@ struct FF {
         a.t = __fadd_rn(a.t, __fadd_rn(s.l, e));
     }
     __device__ static __forceinline__ void msub(Acc& a, T x, T y) { mac(a, {-x.h, -x.l}, y); }
-    // a += x: TwoSum of the high parts, the rest into a.t.
-    __device__ static __forceinline__ void add(Acc& a, T x) {
-        const ff s = two_sum(a.s, x.h);
-        a.s = s.h;
-        a.t = __fadd_rn(a.t, __fadd_rn(s.l, x.l));
-    }
     __device__ static __forceinline__ T fin(Acc a) { return two_sum(a.s, a.t); }
 
     __device__ static __forceinline__ T mul(T a, T b) {
@@ -205,7 +192,6 @@ struct F32 {
         float v;
     };
     static constexpr bool kConv = true;
-    static constexpr bool kAddBLast = true;
 
     // Conversions by bit manipulation (FF::split's high part truncates to 24
     // bits; FF::widen is exact): GB300 runs F2F conversions with a double
@@ -222,7 +208,6 @@ struct F32 {
     __device__ static __forceinline__ Acc acc0() { return {0.f}; }
     __device__ static __forceinline__ void mac(Acc& a, T x, T y) { a.v = __fmaf_rn(x, y, a.v); }
     __device__ static __forceinline__ void msub(Acc& a, T x, T y) { a.v = __fmaf_rn(-x, y, a.v); }
-    __device__ static __forceinline__ void add(Acc& a, T x) { a.v = __fadd_rn(a.v, x); }
     __device__ static __forceinline__ T fin(Acc a) { return a.v; }
 
     __device__ static __forceinline__ T mul(T a, T b) { return __fmul_rn(a, b); }

@@ -17,8 +17,8 @@
 // memory the box lands as slot[i][lane], so lane l reads its column from
 // slot + l + 32*i without bank conflicts.
 //
-// Item order, forward sweep (row q): d_q, A_q and B_q columns 0..m-1 (see
-// fwd_item), C_q columns -- the order the row consumes them: R = B - A C'_{q-1}
+// Item order, forward sweep (row q): d_q, B_q columns 0..m-1, A_q columns,
+// C_q columns -- the order the row consumes them: R = B - A C'_{q-1}
 // and rhs = d - A y_{q-1} are accumulated column by column of A (C'_{q-1}
 // read from shared memory one row at a time), R is factorised (lu_factor), and
 // y_q and the columns of C'_q are solved one at a time (lu_solve), each
@@ -97,13 +97,13 @@ __device__ __forceinline__ void fence_proxy_async_shared() {
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
 // Block-column loops kept rolled (see lu_rolled) only where that measured
-// faster in this kernel, float-float and FP32 at m = 4 (GB300, 16384
-// systems: 4.48 vs 4.67 ms; 131072: 14.7 vs 15.9 ms); at m = 3, 5, 6 the
-// runtime item bookkeeping of a rolled loop costs more than the smaller
-// code saves.
+// faster in this kernel: float-float at m = 4 (GB300, 16384 systems: 4.48
+// vs 4.67 ms; 131072: 14.7 vs 15.9 ms).  At m = 3, 5, 6, and for the
+// smaller FP32 code at m = 4 (11.6 vs 10.4 ms), the runtime item bookkeeping
+// of a rolled loop costs more than the smaller code saves.
 template <class Num, int M>
 __host__ __device__ constexpr bool staged_rolled() {
-    return lu_rolled<Num>() && M == 4;
+    return lu_rolled<Num>() && sizeof(typename Num::T) == 8 && M == 4;
 }
 // Shared memory of one CTA: the ring (R items of M*32 doubles), C'_{q-1}
 // (M*M*32 raw values) and, with rolled loops, y_{q-1} (M*32).  Sized so that
@@ -127,13 +127,8 @@ __host__ __device__ constexpr int staged_smem_bytes() {
     return (staged_ring<Num, M>() * M + staged_fixed_slots<Num, M>()) * 32 * 8;
 }
 
-// Forward item k of a row: which array and which plane offset.  Items:
-// d_q, then the A and the B columns -- A first when the arithmetic adds B
-// last (thomas_b_last), B first otherwise -- then the C columns.  With A
-// first every item has at least one block column of arithmetic between its
-// issue and its use, even with the 6-item ring of m = 5; with B first the A
-// columns are issued while the (instant) B reads run, and each row starts
-// with a memory latency, which the FP64 solve, bound by its FP64 pipe, hides.
+// Forward item k of a row: which array and which plane offset.  Items: d_q,
+// the B columns, the A columns, then the C columns.
 template <class Num, int M>
 __device__ __forceinline__ const CUtensorMap* fwd_item(const ThomasMaps& mp, int k, int& z) {
     if (k == 0) {
@@ -142,11 +137,11 @@ __device__ __forceinline__ const CUtensorMap* fwd_item(const ThomasMaps& mp, int
     }
     if (k <= M) {
         z = (k - 1) * M;
-        return thomas_b_last<Num, M>() ? &mp.a : &mp.b;
+        return &mp.b;
     }
     if (k <= 2 * M) {
         z = (k - 1 - M) * M;
-        return thomas_b_last<Num, M>() ? &mp.b : &mp.a;
+        return &mp.a;
     }
     z = (k - 1 - 2 * M) * M;
     return &mp.c;
@@ -298,28 +293,13 @@ PBT_UNROLL
             for (int j = 0; j < M; ++j) {
                 const double* p = take();
 PBT_UNROLL
-                for (int i = 0; i < M; ++i) {
-                    const T b = Num::in(p + 32 * i);
-                    if constexpr (thomas_b_last<Num, M>())
-                        Num::add(r[i][j], b);
-                    else
-                        r[i][j] = Num::acc(b);
-                }
+                for (int i = 0; i < M; ++i) r[i][j] = Num::acc(Num::in(p + 32 * i));
                 const CUtensorMap* nm = fwd_next(q, k0 + j, nrow_, nz);
                 give(nm, nrow_, nz);
             }
         };
-        if constexpr (thomas_b_last<Num, M>()) {
-PBT_UNROLL
-            for (int i = 0; i < M; ++i)
-PBT_UNROLL
-                for (int j = 0; j < M; ++j) r[i][j] = Num::acc0();
-            a_cols(1);
-            b_cols(1 + M);
-        } else {
-            b_cols(1);
-            a_cols(1 + M);
-        }
+        b_cols(1);
+        a_cols(1 + M);
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
         lu_solve<Num, M>(lu, xd, y);
