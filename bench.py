@@ -24,8 +24,9 @@ bytes per launch), `plain_fp64` (also against the FP64 FMA rate, which is
 what binds plain FP64 on GB300), `cpu_baseline` (the oracle port of the
 reference CPU path on the host cores, on a bounded sample), `variants` (the
 two-stage P = 16 split of the same batch, the long-line case m = 4,
-nsys = 256, N = 32768, P = 128, and the small case m = 3, nsys = 1024,
-N = 128, P = 4 timed with L2 flushed), `mixed_precision`, `adjoint`,
+nsys = 256, N = 32768, P = 128, the small case m = 3, nsys = 1024,
+N = 128, P = 4 timed with L2 flushed, and the pencil batch as periodic lines,
+P = 2), `mixed_precision`, `adjoint`,
 `uneven_batch`, `clocks` (nvidia-smi sampled during the timed region).
 `--sections` limits the extra sections (e.g. `--sections main`).
 
@@ -54,10 +55,11 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 M, NSYS, NROW, NSEG, DELTA, SEED = 5, 65536, 256, 1, 1.2, 20240101
-VARIANTS = [  # name, m, nsys, nrow, nseg, delta
-    ("pencil_P16", 5, 65536, 256, 16, 1.2),
-    ("long_lines_P128", 4, 256, 32768, 128, 1.2),
-    ("small_P4", 3, 1024, 128, 4, 2.0),  # 34.6 MB: fits in L2, timed with L2 flushed before each solve
+VARIANTS = [  # name, m, nsys, nrow, nseg, delta, cyclic
+    ("pencil_P16", 5, 65536, 256, 16, 1.2, False),
+    ("long_lines_P128", 4, 256, 32768, 128, 1.2, False),
+    ("small_P4", 3, 1024, 128, 4, 2.0, False),  # 34.6 MB: fits in L2, timed with L2 flushed before each solve
+    ("pencil_cyclic_P2", 5, 65536, 256, 2, 1.2, True),  # periodic lines (btdma_many_cycl), two segments
 ]
 L2_FIT_BYTES = 256 << 20  # inputs below this are timed with an L2 flush before every solve
 # DRAM bytes (read + write) per block row of k_thomas<FF,5> from ncu
@@ -389,6 +391,7 @@ def run_ours(args):
     import torch
 
     import pascal_btdma_gb300 as pbt
+    from pascal_btdma_gb300 import synth
 
     ws, rank, local = dist_info()
     if ws > 1:
@@ -486,30 +489,39 @@ def run_ours(args):
         p.destroy()
     del a, b, c, d0, hA, hB, hC, hD, keep, w, out_h
     torch.cuda.empty_cache()
-    for name, vm, vns, vn, vp, vdelta in (VARIANTS if "variants" in args.sections else []):
-        vw, _ = make_workload(vm, vns, vn, vdelta, dev)
+    for name, vm, vns, vn, vp, vdelta, vcyc in (VARIANTS if "variants" in args.sections else []):
+        if vcyc:
+            vw = synth.fill(synth.DOMINANT, vm, vns, vn, seed=SEED, delta=vdelta, flags=0)  # A_0, C_{N-1} couple the ends
+        else:
+            vw, _ = make_workload(vm, vns, vn, vdelta, dev)
+        vsolve = pbt.solve_cyclic if vcyc else solve
         va, vb, vc, vd = (torch.from_numpy(x).to(dev) for x in vw.arrays)
         vrows = vns * vn
-        entry = {"m": vm, "nsys": vns, "nrow": vn, "nseg": vp,
+        entry = {"m": vm, "nsys": vns, "nrow": vn, "nseg": vp, "cyclic": vcyc,
                  "l2": "flushed before each solve" if vrows * bytes_per_row(vm) < L2_FIT_BYTES else "inputs > L2"}
         xs = {}
         for prec in ("ff", "fp64"):
-            vplan = pbt.BtdmaGpuPlan().create(vm, vns, vn, vp, precision=prec)
+            vplan = pbt.BtdmaGpuPlan().create(vm, vns, vn, vp, precision=prec, cyclic=vcyc)
             ksteps = max(3, args.steps // 2)
             small = vrows * bytes_per_row(vm) < L2_FIT_BYTES
             if small:
-                vs = time_device_flushed(vplan, (va, vb, vc), vd, vm, vns, vn, ksteps, 3, dev, solve)
+                vs = time_device_flushed(vplan, (va, vb, vc), vd, vm, vns, vn, ksteps, 3, dev, vsolve)
             else:
-                vs = time_device(vplan, (va, vb, vc), [vd], vm, vns, vn, ksteps, 3, ws, dev, solve)
+                vs = time_device(vplan, (va, vb, vc), [vd], vm, vns, vn, ksteps, 3, ws, dev, vsolve)
             vs = max_over_ranks(vs, ws, dev)
             xs[prec] = vd.clone()
-            t = pbt.solve_noncyclic_profiled(vplan, va, vb, vc, xs[prec], vm, vns, vn)
+            if vcyc:
+                vsolve(vplan, va, vb, vc, xs[prec], vm, vns, vn)
+                t = None
+            else:
+                t = pbt.solve_noncyclic_profiled(vplan, va, vb, vc, xs[prec], vm, vns, vn)
             entry[prec] = {
                 "block_rows_per_s": ws * vrows * ksteps / vs,
                 "ms_per_step": vs / ksteps * 1e3,
                 "algorithmic_gbs": vrows * bytes_per_row(vm) / (vs / ksteps) / 1e9,
-                "phases_ms": {"local": t.local_compute * 1e3, "reduced": t.reduced_compute * 1e3,
-                              "update": t.update_compute * 1e3},
+                "phases_ms": None if t is None else {"local": t.local_compute * 1e3,
+                                                     "reduced": t.reduced_compute * 1e3,
+                                                     "update": t.update_compute * 1e3},
             }
             vplan.destroy()
         entry["ff_rel_err_vs_fp64"] = rel_err_vs(xs["ff"], xs["fp64"], vm, vns, vn)

@@ -17,6 +17,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -56,6 +57,11 @@ struct pbt_plan {
     // residual E, convergence statistic, and the outcome of the last solve.
     double* rx = nullptr;
     double* re_ = nullptr;
+    // Two-stage plans over few, long lines: the reduced system (identity
+    // diagonal blocks `rb`) is solved by the same two-stage method through a
+    // plan of its own instead of one thread per system.
+    pbt_plan* sub = nullptr;
+    double* rb = nullptr;
     // PBT_FLAG_CPU_LAYOUT: the inputs in the GPU layout the kernels read.
     double* la = nullptr;
     double* lb = nullptr;
@@ -272,6 +278,33 @@ cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveA
     return run_thomas(arith, m, g);
 }
 
+// Whether a two-stage plan solves its reduced system (nsys lines of `rn`
+// rows) by the two-stage method again: when the lines are long and so few
+// that one thread per line would leave the GPU nearly idle (GB300, m = 4,
+// 256 lines of 32768 rows, P = 128: the 256-row reduced solve took 1.3 of
+// 6.1 ms with 8 warps on 152 SMs).  Its segments have kSubSegRows rows.
+constexpr int kSubSegRows = 8;
+bool recursive_reduced(int nsys, int rn, int sms) {
+    const int warps = (nsys + 31) / 32;
+    return rn >= 8 * kSubSegRows && warps < 4 * (sms > 0 ? sms : 152);
+}
+
+// Identity blocks for every (system, row) of a {nsys, rn, m*m} array in the
+// reference GPU layout.
+int fill_identity(double* rb, int m, int nsys, int rn) {
+    const size_t plane = (size_t)nsys * rn;
+    cudaError_t e = cudaMemset(rb, 0, plane * m * m * sizeof(double));
+    if (e == cudaSuccess) {
+        double* ones = static_cast<double*>(std::malloc(plane * sizeof(double)));
+        if (!ones) return fail(PBT_ENOMEM, "plan: host buffer for the identity blocks");
+        for (size_t i = 0; i < plane; ++i) ones[i] = 1.0;
+        for (int i = 0; i < m && e == cudaSuccess; ++i)
+            e = cudaMemcpy(rb + (size_t)(i + m * i) * plane, ones, plane * sizeof(double), cudaMemcpyHostToDevice);
+        std::free(ones);
+    }
+    return e == cudaSuccess ? PBT_OK : cuda_fail(e, "plan: identity blocks of the reduced system");
+}
+
 PBT_DISPATCH(run_modi, launch_modi)
 PBT_DISPATCH(run_reduced, launch_reduced)
 PBT_DISPATCH(run_reduced_cyclic, launch_reduced_cyclic)
@@ -332,6 +365,10 @@ int validate(const pbt_plan_desc& d) {
 }
 
 void free_plan(pbt_plan* p) {
+    if (p->sub) pbt_plan_destroy(p->sub);
+    p->sub = nullptr;
+    cudaFree(p->rb);
+    p->rb = nullptr;
     cudaFree(p->la);
     cudaFree(p->lb);
     cudaFree(p->lc);
@@ -539,8 +576,26 @@ int solve_core(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
         if ((e = mark(1)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
         if ((e = mark(2)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
         pbt::SolveArgs g2 = make_args(p, a, b, c, d, s, nsys);
-        e = cyclic ? run_reduced_cyclic(arith_of(ds.precision), m, g2) : run_reduced(arith_of(ds.precision), m, g2);
-        if (e != cudaSuccess) return cuda_fail(e, "reduced-stage launch");
+        if (!cyclic && p->sub) {
+            // The reduced rows are raw values of the arithmetic; the sub-plan
+            // reads and writes FP64, so float-float pairs are widened first
+            // and the reduced solution split back after.
+            const bool ff = arith_of(ds.precision) == kFF;
+            const size_t rr = (size_t)nsys * 2 * ds.nseg;
+            if (ff) {
+                if ((e = pbt::launch_ff_raw_f64(p->ra, rr * m * m, 1, s)) != cudaSuccess ||
+                    (e = pbt::launch_ff_raw_f64(p->rc, rr * m * m, 1, s)) != cudaSuccess ||
+                    (e = pbt::launch_ff_raw_f64(p->rd, rr * m, 1, s)) != cudaSuccess)
+                    return cuda_fail(e, "reduced system to FP64");
+            }
+            rc = solve_core(p->sub, p->ra, p->rb, p->rc, p->rd, m, nsys, 2 * ds.nseg, false, nullptr, s);
+            if (rc) return rc;
+            if (ff && (e = pbt::launch_ff_raw_f64(p->rd, rr * m, 0, s)) != cudaSuccess)
+                return cuda_fail(e, "reduced solution to float-float");
+        } else {
+            e = cyclic ? run_reduced_cyclic(arith_of(ds.precision), m, g2) : run_reduced(arith_of(ds.precision), m, g2);
+            if (e != cudaSuccess) return cuda_fail(e, "reduced-stage launch");
+        }
         if ((e = mark(3)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
         e = run_update(arith_of(ds.precision), m, g);
         if (e != cudaSuccess) return cuda_fail(e, "update-stage launch");
@@ -619,6 +674,19 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
         if ((rc = alloc(p, &p->lc, mm * rows))) goto fail_out;
         if ((rc = alloc(p, &p->ld, (size_t)d.m * rows))) goto fail_out;
     }
+    if (!p->thomas && !cyclic && d.precision != PBT_PREC_FP32_REFINE &&
+        recursive_reduced(d.nsys, 2 * d.nseg, p->sms)) {
+        // The reduced system: nsys lines of 2*nseg rows, B = I.
+        const int rn = 2 * d.nseg;
+        if ((rc = alloc(p, &p->rb, mm * rrows))) goto fail_out;
+        if ((rc = fill_identity(p->rb, d.m, d.nsys, rn))) goto fail_out;
+        pbt_plan_desc sd = d;
+        sd.nrow = rn;
+        sd.nseg = rn / kSubSegRows;
+        sd.flags = 0;
+        if ((rc = pbt_plan_create_ex(&p->sub, &sd))) goto fail_out;
+        p->bytes += p->sub->bytes;
+    }
     if (d.precision == PBT_PREC_FP32_REFINE) {
         const size_t nv = (size_t)d.m * rows;
         if ((rc = alloc(p, &p->rx, nv))) goto fail_out;
@@ -690,11 +758,16 @@ int pbt_plan_status(pbt_plan* p, long long* nsingular) {
     if (rc) return rc;
     cudaError_t e = cudaStreamSynchronize(p->last_stream);
     if (e != cudaSuccess) return cuda_fail(e, "plan_status: stream synchronize");
+    // The plan's status word and those of its reduced-system plans.
     unsigned long long v = 0;
-    e = cudaMemcpy(&v, p->status, sizeof v, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "plan_status: read");
-    e = cudaMemset(p->status, 0, sizeof v);
-    if (e != cudaSuccess) return cuda_fail(e, "plan_status: reset");
+    for (pbt_plan* q = p; q != nullptr; q = q->sub) {
+        unsigned long long w = 0;
+        e = cudaMemcpy(&w, q->status, sizeof w, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "plan_status: read");
+        e = cudaMemset(q->status, 0, sizeof w);
+        if (e != cudaSuccess) return cuda_fail(e, "plan_status: reset");
+        v += w;
+    }
     const unsigned long long stalls = v / pbt::kStallMark;
     v %= pbt::kStallMark;
     if (nsingular) *nsingular = (long long)v;

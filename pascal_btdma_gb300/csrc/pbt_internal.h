@@ -80,6 +80,8 @@ template <int M> cudaError_t launch_accumulate(const SolveArgs& g, double* X, co
 // Layout conversion for PBT_FLAG_CPU_LAYOUT plans (pbt_layout.cu): E elements
 // per (system, row); dir 0: CPU layout src -> GPU layout dst, 1: back.
 cudaError_t launch_layout(const double* src, double* dst, int E, int nsys, int nrow, int dir, cudaStream_t s);
+// In place, n 8-byte slots: raw float-float pairs -> FP64 (to_f64 = 1) or back.
+cudaError_t launch_ff_raw_f64(double* x, size_t n, int to_f64, cudaStream_t s);
 
 // Records the message returned by pbt_last_error_string() on this thread and
 // returns `code` (defined in pbt_api.cpp).

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include "pbt_internal.h"
+#include "pbt_num.cuh"
 
 namespace pbt {
 
@@ -58,7 +59,28 @@ __global__ void __launch_bounds__(kThreads) k_layout(const double* __restrict__ 
     }
 }
 
+// In place: raw float-float pairs (8-byte slots, as the kernels keep their
+// intermediates) <-> FP64 values.  The pair (h, l) has |l| <= ulp(h)/2, so
+// h + l is exact in FP64; back, FF::split keeps 47 bits.
+__global__ void k_ff_raw_f64(double* x, size_t n, int to_f64) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (to_f64) {
+            x[i] = FF::join(FF::lds(x + i));
+        } else {
+            const double v = x[i];
+            FF::sts(x + i, FF::split(v));
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_ff_raw_f64(double* x, size_t n, int to_f64, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const size_t blocks = (n + kThreads - 1) / kThreads;
+    k_ff_raw_f64<<<(unsigned)(blocks < 4096 ? blocks : 4096), kThreads, 0, s>>>(x, n, to_f64);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_layout(const double* src, double* dst, int E, int nsys, int nrow, int dir, cudaStream_t s) {
     if (E <= 0 || nsys <= 0 || nrow <= 0) return cudaSuccess;

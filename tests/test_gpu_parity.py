@@ -237,3 +237,16 @@ def test_refine_stops_at_max_iter(cuda):
         pbt.solve_noncyclic(plan, a, b, c, d, 3, 64, 40)
         iters, corr = plan.refine_info()
     assert iters == 3 and corr > 0
+
+
+@pytest.mark.parametrize("m,nsys,nrow,nseg", [(3, 64, 1024, 64), (4, 100, 600, 50), (5, 40, 4096, 256)])
+@pytest.mark.parametrize("prec,tol", PREC_TOL)
+def test_recursive_reduced_solve(cuda, m, nsys, nrow, nseg, prec, tol):
+    """Few long lines: the plan solves its 2P-row reduced system with the
+    two-stage method again (a reduced-system plan of 8-row segments, and for
+    2P >= 512 one more level)."""
+    w = synth.dominant(m, nsys, nrow, seed=300 + m, delta=1.5)
+    (_, _, _, D), singular = gpu_solve(w, nseg, precision=prec)
+    ref = oracle_solve(w, nseg)
+    assert singular == 0
+    assert per_system_relerr(m, nsys, nrow, D, ref.D) <= tol
