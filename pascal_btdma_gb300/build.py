@@ -35,7 +35,7 @@ MAX_BLOCK = 10
 # Families of kernels instantiated per block size: (source, object stem).
 PER_M_SOURCES = [("pbt_inst.cu", "F64"), ("pbt_inst.cu", "FF"), ("pbt_inst.cu", "F32")]
 HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu", "pbt_noalloc.cu", "pbt_batch.cpp", "pbt_batch_f64.cu",
-                "pbt_batch_ff.cu", "pbt_layout.cu"]
+                "pbt_batch_ff.cu", "pbt_layout.cu", "pbt_shared.cu"]
 
 
 def _nvcc() -> str:

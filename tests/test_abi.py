@@ -21,7 +21,7 @@ def declared(header: str) -> set[str]:
 
 
 @pytest.mark.parametrize("header,loader", [("pbt.h", N.lib), ("pbt_probe.h", N.lib), ("pbt_batch.h", N.lib),
-                                           ("pbt_synth.h", N.synth_lib)])
+                                           ("pbt_shared.h", N.lib), ("pbt_synth.h", N.synth_lib)])
 def test_every_declared_symbol_is_exported(header, loader):
     lib = loader()
     names = declared(header)
@@ -37,6 +37,9 @@ def test_python_signatures_cover_header():
     from pascal_btdma_gb300 import batch
 
     assert declared("pbt_batch.h") == set(batch.BATCH_SIGNATURES)
+    from pascal_btdma_gb300 import shared
+
+    assert declared("pbt_shared.h") == set(shared.SHARED_SIGNATURES)
 
 
 def test_python_constants_match_header():
@@ -170,3 +173,35 @@ def test_cpu_layout_index_helpers_match_oracle_conversion():
     for sys, row, p, q in [(0, 0, 0, 0), (4, 3, 2, 1), (2, 1, 1, 2)]:
         assert c[pbt.cpu_matrix_index(sys, row, p, q, nsys, m)] == g[pbt.matrix_index(sys, row, p, q, nsys, nrow, m)]
         assert cv[pbt.cpu_vector_index(sys, row, p, nsys, m)] == gv[pbt.vector_index(sys, row, p, nsys, nrow)]
+
+
+def test_shared_create_checks_before_the_gpu():
+    """Bad sizes and a singular shared matrix are refused on the host."""
+    import numpy as np
+
+    from pascal_btdma_gb300 import shared
+
+    with pytest.raises(ValueError):
+        shared.SharedMatrix(11, 4, np.zeros(4 * 121), np.zeros(4 * 121), np.zeros(4 * 121))
+    with pytest.raises(ValueError):
+        shared.SharedMatrix(2, 4, np.zeros(3), np.zeros(16), np.zeros(16))
+    m, nrow = 2, 4
+    a, b, c = (np.zeros(nrow * m * m) for _ in range(3))  # B = 0: the first pivot is zero
+    with pytest.raises(pbt.SingularBlockError):
+        shared.SharedMatrix(m, nrow, a, b, c)
+
+
+def test_heat3d_blocks_match_reference_stencil():
+    """The heat3d blocks (build_matrix_kernel): interior rows hold the
+    fourth-order stencil [-1, 16, -30, 16, -1]/12 scaled into sigma units."""
+    import numpy as np
+
+    from pascal_btdma_gb300 import shared
+
+    nblk, sigma = 4, 0.1
+    a, b, c = shared.heat3d_blocks(nblk, sigma)
+    el = lambda x, q, i, j: x[q + nblk * (i + 2 * j)]  # noqa: E731
+    q = 1  # interior: point 2q (i = 0) row of the assembled matrix, columns 2q-2 .. 2q+2
+    row0 = [el(a, q, 0, 0), el(a, q, 0, 1), el(b, q, 0, 0), el(b, q, 0, 1), el(c, q, 0, 0), el(c, q, 0, 1)]
+    assert np.allclose(row0, [sigma, -16 * sigma, 1 + 30 * sigma, -16 * sigma, sigma, 0.0])
+    assert el(a, 0, 0, 0) == 0.0 and el(c, nblk - 1, 1, 1) == 0.0
