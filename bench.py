@@ -27,7 +27,10 @@ two-stage P = 16 split of the same batch, the long-line case m = 4,
 nsys = 256, N = 32768, P = 128, the small case m = 3, nsys = 1024,
 N = 128, P = 4 timed with L2 flushed, and the pencil batch as periodic lines,
 P = 2), `mixed_precision`, `adjoint`,
-`uneven_batch`, `clocks` (nvidia-smi sampled during the timed region).
+`uneven_batch`, `shared_lines` (one heat3d ADI step, three sweeps of
+shared-matrix lines in place in a 516^3 haloed field, against the general
+solver with pack/unpack), `clocks` (nvidia-smi sampled during the timed
+region).
 `--sections` limits the extra sections (e.g. `--sections main`).
 
 Under torchrun (N > 1) every rank solves its own full batch (weak scaling,
@@ -81,6 +84,8 @@ ADJ = dict(m=4, nsys=16384, nrow=512, delta=1.5, segs=(8, 1), pressure_tiles=16)
 # {2, 3, 4, 5}, delta = 1.5; one persistent launch per sweep, 100 sweeps in a
 # CUDA graph; tuning by the autotuner; against one plain launch per (m, N).
 UNEVEN = dict(nsys=32768, nmin=16, nmax=4096, mmin=2, mmax=5, delta=1.5, sweeps=100)
+# heat3d-style ADI step: a 512^3 field with a halo of 2, lines of 256 blocks of 2 points
+SHARED = dict(n=512, halo=2, sigma=0.05, steps=5)
 METRIC = "block-rows/s (chosen method at <=1e-10 rel err vs plain FP64)"
 DATA = "synthetic (seeded Philox4x32-10, diagonally dominant, delta=1.2)"
 
@@ -90,6 +95,78 @@ def workload_config(ws: int) -> dict:
     return {"workload": f"pencil batch m={M}, nsys={NSYS}, N={NROW}, P={NSEG}", "m": M, "nsys": NSYS,
             "nrow": NROW, "nseg": NSEG, "l2": "inputs 11.4 GB > L2 (no flush needed)",
             "parallelism": f"replicas x{ws}"}
+
+
+def run_shared(dev) -> dict:
+    """Shared-matrix lines (include/pbt_shared.h): the three sweeps of one
+    heat3d ADI step solved in place in the haloed field, against one sweep of
+    the general solver on the same lines packed into the reference layout
+    (matrix replicated per line; pack and unpack by PyTorch copies)."""
+    import torch
+
+    import pascal_btdma_gb300 as pbt
+    from pascal_btdma_gb300 import shared
+
+    cfg = SHARED
+    n, h = cfg["n"], cfg["halo"]
+    nblk, m = n // 2, 2
+    field = torch.rand((n + 2 * h,) * 3, dtype=torch.float64, device=dev)
+    interior = field[h:-h, h:-h, h:-h]
+    st = interior.stride()
+    a, b, c = shared.heat3d_blocks(nblk, cfg["sigma"])
+    rows = n * n * nblk  # block rows per sweep
+    sweeps = []
+    for axis in (2, 1, 0):  # x, y, z as heat3d orders them
+        outer, inner = [x for x in range(3) if x != axis]
+        sweeps.append(shared.Lines(n, n, st[inner], st[outer], 2 * st[axis], st[axis]))
+    s0 = torch.cuda.current_stream()
+    out = {"field": [n + 2 * h] * 3, "halo": h, "m": m, "nblk": nblk, "lines_per_sweep": n * n,
+           "bytes_per_block_row": 4 * m * 8,
+           "bytes_note": "rhs read, y written and read back, x written: 4*m doubles per block row per sweep"}
+    for prec in ("ff", "fp64"):
+        with shared.SharedMatrix(m, nblk, a, b, c, precision=prec) as sm:
+            for L in sweeps:
+                sm.solve(interior, interior, L)
+            per = []
+            for L in sweeps:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s0)
+                for _ in range(cfg["steps"]):
+                    sm.solve(interior, interior, L)
+                e1.record(s0)
+                torch.cuda.synchronize()
+                per.append(e0.elapsed_time(e1) / 1e3 / cfg["steps"])
+        gbs = [rows * out["bytes_per_block_row"] / t / 1e9 for t in per]
+        out[prec] = {"ms_per_adi_step": sum(per) * 1e3,
+                     "ms_per_sweep_xyz": [t * 1e3 for t in per],
+                     "block_rows_per_s": 3 * rows / sum(per),
+                     "algorithmic_gbs_xyz": gbs}
+    # General solver on the z sweep's lines: pack, solve (FF), unpack.
+    nsys = n * n
+    rep = [torch.from_numpy(x).to(dev).view(-1, 1).expand(-1, nsys).contiguous().view(-1) for x in (a, b, c)]
+    d = torch.empty(m * nblk * nsys, dtype=torch.float64, device=dev)
+    with pbt.BtdmaGpuPlan() as pl:
+        pl.create(m, nsys, nblk, 1, precision="ff")
+
+        def general_sweep():
+            # field axis 0 -> (point = 2q + i, s_out, s_in) -> reference layout sys + nsys*(q + nblk*i)
+            d.view(m, nblk, n, n).copy_(interior.unflatten(0, (nblk, m)).permute(1, 0, 2, 3))
+            pbt.solve_noncyclic(pl, *rep, d, m, nsys, nblk)
+            interior.unflatten(0, (nblk, m)).copy_(d.view(m, nblk, n, n).permute(1, 0, 2, 3))
+
+        general_sweep()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s0)
+        for _ in range(cfg["steps"]):
+            general_sweep()
+        e1.record(s0)
+        torch.cuda.synchronize()
+        gen = e0.elapsed_time(e1) / 1e3 / cfg["steps"]
+    out["general_ff_pack_solve_unpack_ms_per_sweep"] = gen * 1e3
+    out["speedup_ff_vs_general_ff"] = gen / (out["ff"]["ms_per_adi_step"] / 3e3)
+    del field, interior, rep, d
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_uneven(dev, log=None) -> dict:
@@ -616,6 +693,7 @@ def run_ours(args):
         del Ap, Bp, Cp, Dp, aw
         torch.cuda.empty_cache()
     uneven = run_uneven(dev) if "uneven" in args.sections else {}
+    shared_lines = run_shared(dev) if "shared" in args.sections else {}
 
     result = {
         "metric": METRIC,
@@ -656,6 +734,7 @@ def run_ours(args):
         "mixed_precision": mixed,
         "adjoint": adjoint,
         "uneven_batch": uneven,
+        "shared_lines": shared_lines,
     }
     if rank == 0:
         if "cpu" in args.sections:
@@ -716,11 +795,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--sections", default="all",
                     help="comma list of extra sections to run beside the headline: variants, mixed, adjoint, "
-                         "uneven, cpu; 'all' (default) or 'main' (headline only)")
+                         "uneven, shared, cpu; 'all' (default) or 'main' (headline only)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    known = {"variants", "mixed", "adjoint", "uneven", "cpu"}
+    known = {"variants", "mixed", "adjoint", "uneven", "shared", "cpu"}
     if args.sections == "all":
         args.sections = known
     elif args.sections == "main":

@@ -50,10 +50,14 @@ typedef struct pbt_lines {
 /* Factorise the matrix every line shares: a, b, c are HOST arrays of one
  * system, nrow*m*m doubles each, element (i, j) of row q at q + nrow*(i + m*j)
  * (the reference layout with nsys = 1); A_0 and C_{nrow-1} are ignored.  The
- * factors go to device memory on the current device.  Returns PBT_ESINGULAR
- * (with nothing created) if a zero pivot is met, PBT_EINVAL for bad sizes
- * (1 <= m <= PBT_MAX_BLOCK, nrow >= 2). */
-int pbt_shared_create(pbt_shared** s, int m, int nrow, const double* a, const double* b, const double* c);
+ * factorisation runs on the host in FP64; the factors go to device memory on
+ * the current device.  precision: PBT_PREC_FP64 (the solve in FP64) or
+ * PBT_PREC_FF (the solve in float-float arithmetic on the FP32 pipes, ~47
+ * significant bits; factors must lie below 2^127 in magnitude), anything else
+ * PBT_EUNSUPPORTED.  Returns PBT_ESINGULAR (with nothing created) if a zero
+ * pivot is met, PBT_EINVAL for bad sizes (1 <= m <= PBT_MAX_BLOCK, nrow >= 2). */
+int pbt_shared_create(pbt_shared** s, int m, int nrow, const double* a, const double* b, const double* c,
+                      int precision);
 
 /* x <- M^{-1} rhs for every line (device arrays; x may equal rhs).  The
  * solve uses x as its scratch: rows of x hold intermediate values until the

@@ -10,7 +10,12 @@
 // at each step, the multipliers, the U rows and 1/U_kk.  A line's solve is
 // then  y_q = R_q^{-1}(d_q - A_q y_{q-1}),  x_q = y_q - C'_q x_{q+1}:
 // about 3*m^2 multiply-adds a row, every line reading the same factors (a
-// broadcast from L1/L2) and only its own right-hand side and solution.
+// broadcast from L1/L2) and only its own right-hand side and solution.  At
+// m = 2 that is 12 FMAs a row against 64 bytes of traffic, over the FP64
+// pipe's balance point on GB300 (626 G FMA/s against 6.7 TB/s), so the
+// solve also runs in float-float arithmetic on the FP32 pipes (PBT_PREC_FF:
+// factors stored as (h, l) float pairs, right-hand sides split on load, y
+// kept as raw pairs in x between the sweeps, x joined back to FP64).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -23,10 +28,12 @@
 
 #include "../../include/pbt_shared.h"
 #include "pbt_internal.h"
+#include "pbt_num.cuh"
 
 struct pbt_shared {
-    int m = 0, nrow = 0;
-    double* fac = nullptr;        // per row q: A_q, the factors of R_q, C'_q (3*m*m doubles, element (i,j) at i + m*j)
+    int m = 0, nrow = 0, precision = PBT_PREC_FP64;
+    double* fac = nullptr;        // per row q: A_q, the factors of R_q, C'_q (3*m*m 8-byte slots, element (i,j) at
+                                  // i + m*j): FP64 values, or float-float pairs (h, l) for PBT_PREC_FF
     long long* piv = nullptr;     // per row q: 4 bits per elimination step, the row swapped in
     unsigned magic = 0x50425453u;  // "PBTS"
 };
@@ -34,81 +41,291 @@ struct pbt_shared {
 namespace {
 
 constexpr unsigned kSharedMagic = 0x50425453u;
-constexpr int kSharedThreads = 128;
+constexpr int kSharedWarps = 4;
+constexpr int kSharedThreads = 32 * kSharedWarps;
+
+// A warp owns 32 consecutive lines and walks them in chunks of K block rows
+// (K*M <= 16 doubles, 128 bytes of a line).  A chunk is staged in shared
+// memory, [line][K*M] with an odd row stride S (no bank conflicts), by
+// coalesced loads whatever the layout:
+//   contiguous lines (elem_stride 1, row_stride M: the sweep along the fast
+//     axis): each half-warp reads one line's chunk, 128 contiguous bytes;
+//   otherwise: lane = line, one load per element of the chunk, 32 lines
+//     side by side (256 contiguous bytes when stride_inner is 1).
+// Each lane then runs its own line's recurrence on the tile and the tile is
+// written back the same way.  The forward sweep leaves y in x; the last chunk
+// turns around in shared memory, and the backward sweep reloads the other
+// chunks last to first.  Latency is hidden by warps, not by prefetching in a
+// warp: registers are capped so that as many blocks fit on an SM as the
+// arithmetic allows without spills (shared_min_blocks).
+template <int M>
+struct SharedTile {
+    static constexpr int K = 16 / M > 0 ? 16 / M : 1;
+    static constexpr int KM = K * M;
+    static constexpr int S = KM | 1;
+};
+
+// Blocks an SM must hold (the register cap), as many as fit without spills.
+template <class Num, int M>
+__host__ __device__ constexpr int shared_min_blocks() {
+    return Num::kConv ? (M <= 2 ? 8 : M <= 4 ? 6 : 4) : (M <= 4 ? 5 : 4);
+}
+
+// Chunk moves.  fetch() issues a chunk's loads into registers (v: up to 16
+// doubles a lane), deposit() puts them in the tile, store() writes the tile
+// out; a lane's loads all go out before anything waits on them.
+template <int M>
+__device__ __forceinline__ void fetch(const double* src, double* v, long long base, bool live, int nlive, int q0, int kk,
+                                      const pbt_lines& L, bool contiguous) {
+    constexpr int K = SharedTile<M>::K;
+    static_assert(SharedTile<M>::KM <= 16, "a chunk is at most 16 doubles of a line");
+    const int lane = threadIdx.x & 31;
+    if (contiguous) {
+        const int len = kk * M, half = lane >> 4, e = lane & 15;
+#pragma unroll
+        for (int it = 0; it < 16; ++it) {
+            const int j = 2 * it + half;
+            const long long bj = __shfl_sync(0xffffffffu, base, j) + (long long)q0 * M + e;
+            v[it] = (j < nlive && e < len) ? src[bj] : 0.0;
+        }
+    } else if (live) {
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            if (u < kk) {
+                const long long r = base + (long long)(q0 + u) * L.row_stride;
+#pragma unroll
+                for (int i = 0; i < M; ++i) v[u * M + i] = src[r + i * L.elem_stride];
+            }
+        }
+    }
+}
 
 template <int M>
-__global__ void __launch_bounds__(kSharedThreads) k_shared(const double* __restrict__ fac,
-                                                           const long long* __restrict__ pivs,
-                                                           const double* rhs, double* x, int nrow, pbt_lines L) {
-    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nsys = (long long)L.nsys_inner * L.nsys_outer;
-    if (s >= nsys) return;
-    const long long s_in = s % L.nsys_inner, s_out = s / L.nsys_inner;
-    const long long base = s_in * L.stride_inner + s_out * L.stride_outer;
-    const double* r = rhs + base;
-    double* o = x + base;
-    double y[M];
-    for (int q = 0; q < nrow; ++q) {
-        const double* Aq = fac + (size_t)q * 3 * M * M;
-        const double* F = Aq + M * M;
-        const long long pq = __ldg(pivs + q);
-        double t[M];
+__device__ __forceinline__ void deposit(const double* v, double* tile, bool live, int nlive, int kk, bool contiguous) {
+    constexpr int K = SharedTile<M>::K, S = SharedTile<M>::S;
+    const int lane = threadIdx.x & 31;
+    if (contiguous) {
+        const int len = kk * M, half = lane >> 4, e = lane & 15;
 #pragma unroll
-        for (int i = 0; i < M; ++i) t[i] = r[q * L.row_stride + i * L.elem_stride];
-        if (q > 0) {
-#pragma unroll
-            for (int i = 0; i < M; ++i)
-#pragma unroll
-                for (int k = 0; k < M; ++k) t[i] = fma(-__ldg(Aq + i + M * k), y[k], t[i]);
+        for (int it = 0; it < 16; ++it) {
+            const int j = 2 * it + half;
+            if (j < nlive && e < len) tile[j * S + e] = v[it];
         }
-        // Replay the elimination of R_q on t, then back-substitute.
+    } else if (live) {
+        double* my = tile + lane * S;
 #pragma unroll
-        for (int k = 0; k < M; ++k) {
-            if (k + 1 < M) {
-                const int p = (int)((pq >> (4 * k)) & 15);
+        for (int u = 0; u < K; ++u)
+            if (u < kk)
 #pragma unroll
-                for (int i = k + 1; i < M; ++i) {
-                    const bool sw = (p == i);
-                    const double a = t[k], b = t[i];
-                    t[k] = sw ? b : a;
-                    t[i] = sw ? a : b;
-                }
-            }
-#pragma unroll
-            for (int i = k + 1; i < M; ++i) t[i] = fma(-__ldg(F + i + M * k), t[k], t[i]);
-        }
-#pragma unroll
-        for (int k = M - 1; k >= 0; --k) {
-            const double xk = t[k] * __ldg(F + k + M * k);
-            y[k] = xk;
-#pragma unroll
-            for (int i = 0; i < k; ++i) t[i] = fma(-__ldg(F + i + M * k), xk, t[i]);
-        }
-#pragma unroll
-        for (int i = 0; i < M; ++i) o[q * L.row_stride + i * L.elem_stride] = y[i];
+                for (int i = 0; i < M; ++i) my[u * M + i] = v[u * M + i];
     }
-    for (int q = nrow - 2; q >= 0; --q) {
-        const double* Cq = fac + (size_t)q * 3 * M * M + 2 * M * M;
-        double t[M];
+    __syncwarp();
+}
+
+template <int M>
+__device__ __forceinline__ void store(double* dst, const double* tile, long long base, bool live, int nlive, int q0,
+                                      int kk, const pbt_lines& L, bool contiguous) {
+    constexpr int K = SharedTile<M>::K, S = SharedTile<M>::S;
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (contiguous) {
+        const int len = kk * M, half = lane >> 4, e = lane & 15;
 #pragma unroll
-        for (int i = 0; i < M; ++i) t[i] = o[q * L.row_stride + i * L.elem_stride];
+        for (int it = 0; it < 16; ++it) {
+            const int j = 2 * it + half;
+            const long long bj = __shfl_sync(0xffffffffu, base, j) + (long long)q0 * M + e;
+            if (j < nlive && e < len) dst[bj] = tile[j * S + e];
+        }
+    } else if (live) {
+        const double* my = tile + lane * S;
 #pragma unroll
-        for (int i = 0; i < M; ++i)
+        for (int u = 0; u < K; ++u) {
+            if (u < kk) {
+                const long long r = base + (long long)(q0 + u) * L.row_stride;
 #pragma unroll
-            for (int k = 0; k < M; ++k) t[i] = fma(-__ldg(Cq + i + M * k), y[k], t[i]);
+                for (int i = 0; i < M; ++i) dst[r + i * L.elem_stride] = my[u * M + i];
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// One stored factor (an 8-byte slot of the factor array) in arithmetic Num.
+template <class Num>
+__device__ __forceinline__ typename Num::T ldf(const double* p);
+template <>
+__device__ __forceinline__ double ldf<pbt::F64>(const double* p) {
+    return __ldg(p);
+}
+template <>
+__device__ __forceinline__ pbt::ff ldf<pbt::FF>(const double* p) {
+    const float2 f = __ldg(reinterpret_cast<const float2*>(p));
+    return {f.x, f.y};
+}
+
+// y = R_q^{-1} (t - A_q y_prev) with the stored factors of R_q (t in, y out).
+template <class Num, int M>
+__device__ __forceinline__ void forward_row(const double* __restrict__ fac, const long long* __restrict__ pivs, int q,
+                                            typename Num::T* t, typename Num::T* y) {
+    using T = typename Num::T;
+    const double* Aq = fac + (size_t)q * 3 * M * M;
+    const double* F = Aq + M * M;
+    const long long pq = __ldg(pivs + q);
+    if (q > 0) {
 #pragma unroll
         for (int i = 0; i < M; ++i) {
-            y[i] = t[i];
-            o[q * L.row_stride + i * L.elem_stride] = t[i];
+            typename Num::Acc a = Num::acc(t[i]);
+#pragma unroll
+            for (int k = 0; k < M; ++k) Num::msub(a, ldf<Num>(Aq + i + M * k), y[k]);
+            t[i] = Num::fin(a);
         }
+    }
+    // Replay the elimination of R_q on t, then back-substitute.
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        if (k + 1 < M) {
+            const int p = (int)((pq >> (4 * k)) & 15);
+#pragma unroll
+            for (int i = k + 1; i < M; ++i) {
+                const unsigned sw = (p == i);
+                const T a = t[k], b = t[i];
+                t[k] = Num::sel(sw, b, a);
+                t[i] = Num::sel(sw, a, b);
+            }
+        }
+#pragma unroll
+        for (int i = k + 1; i < M; ++i) {
+            typename Num::Acc a = Num::acc(t[i]);
+            Num::msub(a, ldf<Num>(F + i + M * k), t[k]);
+            t[i] = Num::fin(a);
+        }
+    }
+#pragma unroll
+    for (int k = M - 1; k >= 0; --k) {
+        const T xk = Num::mul(t[k], ldf<Num>(F + k + M * k));
+        y[k] = xk;
+#pragma unroll
+        for (int i = 0; i < k; ++i) {
+            typename Num::Acc a = Num::acc(t[i]);
+            Num::msub(a, ldf<Num>(F + i + M * k), xk);
+            t[i] = Num::fin(a);
+        }
+    }
+}
+
+// x_q = y_q - C'_q x_{q+1}: t holds y_q in, x is x_{q+1} in and x_q out.
+template <class Num, int M>
+__device__ __forceinline__ void backward_row(const double* __restrict__ fac, int q, const typename Num::T* t,
+                                             typename Num::T* x) {
+    const double* Cq = fac + (size_t)q * 3 * M * M + 2 * M * M;
+    typename Num::T v[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        typename Num::Acc a = Num::acc(t[i]);
+#pragma unroll
+        for (int k = 0; k < M; ++k) Num::msub(a, ldf<Num>(Cq + i + M * k), x[k]);
+        v[i] = Num::fin(a);
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) x[i] = v[i];
+}
+
+// The tile holds FP64 right-hand sides on the way in, raw y values (Num's
+// 8-byte workspace form) between the sweeps and FP64 solutions on the way out.
+template <class Num, int M>
+__global__ void __launch_bounds__(kSharedThreads, (shared_min_blocks<Num, M>())) k_shared(const double* __restrict__ fac,
+                                                           const long long* __restrict__ pivs,
+                                                           const double* rhs, double* x, int nrow, pbt_lines L,
+                                                           int contiguous) {
+    using T = typename Num::T;
+    constexpr int K = SharedTile<M>::K, S = SharedTile<M>::S;
+    __shared__ double tiles[kSharedWarps][32 * S];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long nsys = (long long)L.nsys_inner * L.nsys_outer;
+    const long long s0 = ((long long)blockIdx.x * kSharedWarps + w) * 32;
+    if (s0 >= nsys) return;  // the whole warp
+    double* tile = tiles[w];
+    double* my = tile + lane * S;
+    const long long s = s0 + lane;
+    const bool live = s < nsys;
+    const int nlive = (int)(nsys - s0 < 32 ? nsys - s0 : 32);
+    long long base = 0;
+    if (live) base = (s % L.nsys_inner) * L.stride_inner + (s / L.nsys_inner) * L.stride_outer;
+    const bool cont = contiguous != 0;
+    const int nchunk = (nrow + K - 1) / K;
+    // Steps 0..nchunk-1: forward chunks first to last; then the backward
+    // sweep over chunks nchunk-2 down to 0 (the last chunk turns around in
+    // the tile).
+    const int nsteps = 2 * nchunk - 1;
+    T y[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) y[i] = Num::zero();
+    for (int st = 0; st < nsteps; ++st) {
+        const bool fwd = st < nchunk;
+        const int q0 = (fwd ? st : 2 * nchunk - 2 - st) * K, kk = min(K, nrow - q0);
+        {
+            double v[16];
+            fetch<M>(fwd ? rhs : x, v, base, live, nlive, q0, kk, L, cont);
+            deposit<M>(v, tile, live, nlive, kk, cont);
+        }
+        if (live && fwd) {
+            const bool last = st == nchunk - 1;
+#pragma unroll
+            for (int u = 0; u < K; ++u) {
+                if (u < kk) {
+                    T t[M];
+#pragma unroll
+                    for (int i = 0; i < M; ++i) t[i] = Num::in(my + u * M + i);
+                    forward_row<Num, M>(fac, pivs, q0 + u, t, y);
+                    if (last && u == kk - 1) {  // y of the last row is its solution
+#pragma unroll
+                        for (int i = 0; i < M; ++i) Num::out(my + u * M + i, y[i]);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < M; ++i) Num::sts(my + u * M + i, y[i]);
+                    }
+                }
+            }
+            if (last) {  // turn around in the tile
+#pragma unroll
+                for (int u = K - 2; u >= 0; --u) {
+                    if (u + 1 < kk) {
+                        T t[M];
+#pragma unroll
+                        for (int i = 0; i < M; ++i) t[i] = Num::lds(my + u * M + i);
+                        backward_row<Num, M>(fac, q0 + u, t, y);
+#pragma unroll
+                        for (int i = 0; i < M; ++i) Num::out(my + u * M + i, y[i]);
+                    }
+                }
+            }
+        } else if (live) {
+#pragma unroll
+            for (int u = K - 1; u >= 0; --u) {
+                T t[M];
+#pragma unroll
+                for (int i = 0; i < M; ++i) t[i] = Num::lds(my + u * M + i);
+                backward_row<Num, M>(fac, q0 + u, t, y);
+#pragma unroll
+                for (int i = 0; i < M; ++i) Num::out(my + u * M + i, y[i]);
+            }
+        }
+        store<M>(x, tile, base, live, nlive, q0, kk, L, cont);
     }
 }
 
 template <int M>
 cudaError_t launch_shared(const pbt_shared* sh, const double* rhs, double* x, const pbt_lines& L, cudaStream_t st) {
     const long long nsys = (long long)L.nsys_inner * L.nsys_outer;
-    const long long grid = (nsys + kSharedThreads - 1) / kSharedThreads;
-    k_shared<M><<<(unsigned)grid, kSharedThreads, 0, st>>>(sh->fac, sh->piv, rhs, x, sh->nrow, L);
+    const long long warps = (nsys + 31) / 32;
+    const long long grid = (warps + kSharedWarps - 1) / kSharedWarps;
+    if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const int contiguous = (L.elem_stride == 1 && L.row_stride == M) ? 1 : 0;
+    if (sh->precision == PBT_PREC_FF)
+        k_shared<pbt::FF, M><<<(unsigned)grid, kSharedThreads, 0, st>>>(sh->fac, sh->piv, rhs, x, sh->nrow, L, contiguous);
+    else
+        k_shared<pbt::F64, M><<<(unsigned)grid, kSharedThreads, 0, st>>>(sh->fac, sh->piv, rhs, x, sh->nrow, L,
+                                                                         contiguous);
     return cudaGetLastError();
 }
 
@@ -167,9 +384,12 @@ void host_solve(int m, const double* f, const int* swaps, double* b) {
 
 extern "C" {
 
-int pbt_shared_create(pbt_shared** out, int m, int nrow, const double* a, const double* b, const double* c) {
+int pbt_shared_create(pbt_shared** out, int m, int nrow, const double* a, const double* b, const double* c,
+                      int precision) {
     if (!out) return pbt::set_last_error(PBT_EINVAL, "shared_create: null argument");
     *out = nullptr;
+    if (precision != PBT_PREC_FP64 && precision != PBT_PREC_FF)
+        return pbt::set_last_error(PBT_EUNSUPPORTED, "shared_create: precision must be PBT_PREC_FP64 or PBT_PREC_FF");
     if (m < 1 || m > PBT_MAX_BLOCK || nrow < 2 || !a || !b || !c) {
         char buf[160];
         std::snprintf(buf, sizeof buf, "shared_create: need 1 <= m <= %d, nrow >= 2 and three arrays (m=%d, nrow=%d)",
@@ -213,10 +433,21 @@ int pbt_shared_create(pbt_shared** out, int m, int nrow, const double* a, const 
             std::memcpy(cprev.data(), Cq, mm * sizeof(double));
         }
     }
+    if (precision == PBT_PREC_FF) {
+        // (h, l) = (v rounded to float, the rest rounded to float): |l| <= ulp(h)/2.
+        for (double& v : fac) {
+            if (!(std::fabs(v) < 0x1p127))
+                return pbt::set_last_error(PBT_EINVAL, "shared_create: a factor is outside the float-float range");
+            const float h = (float)v, l = (float)(v - (double)h);
+            float pair[2] = {h, l};
+            std::memcpy(&v, pair, sizeof v);
+        }
+    }
     pbt_shared* s = new (std::nothrow) pbt_shared();
     if (!s) return pbt::set_last_error(PBT_ENOMEM, "shared_create: host allocation failed");
     s->m = m;
     s->nrow = nrow;
+    s->precision = precision;
     cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&s->fac), fac.size() * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&s->piv), piv.size() * sizeof(long long));
     if (e == cudaSuccess)

@@ -27,7 +27,7 @@ class _LinesC(C.Structure):
 
 _P = C.c_void_p
 SHARED_SIGNATURES = {
-    "pbt_shared_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int, _P, _P, _P]),
+    "pbt_shared_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int, _P, _P, _P, C.c_int]),
     "pbt_shared_solve": (C.c_int, [_P, _P, _P, C.POINTER(_LinesC), _P]),
     "pbt_shared_shape": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "pbt_shared_destroy": (C.c_int, [_P]),
@@ -84,18 +84,24 @@ class Lines:
 class SharedMatrix:
     """One block-tridiagonal matrix (nrow block rows of size m) shared by
     every line.  a, b, c: host arrays of one system, element (i, j) of row q
-    at q + nrow*(i + m*j) (A_0 and C_{nrow-1} are ignored)."""
+    at q + nrow*(i + m*j) (A_0 and C_{nrow-1} are ignored).  precision:
+    "fp64" or "ff" (float-float on the FP32 pipes), the arithmetic of the
+    solve; the factorisation is FP64 on the host either way."""
 
-    def __init__(self, m: int, nrow: int, a, b, c):
+    def __init__(self, m: int, nrow: int, a, b, c, precision: str = "fp64"):
+        from . import PRECISIONS
+
+        if precision not in ("fp64", "ff"):
+            raise ValueError(f"precision {precision!r}: SharedMatrix solves in 'fp64' or 'ff'")
         arrs = [np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (a, b, c)]
         for x in arrs:
             if x.size != nrow * m * m:
                 raise ValueError(f"each block array needs nrow*m*m = {nrow * m * m} values")
         h = _P()
-        _raise(_lib().pbt_shared_create(C.byref(h), int(m), int(nrow), *(x.ctypes.data for x in arrs)),
-               "SharedMatrix")
+        _raise(_lib().pbt_shared_create(C.byref(h), int(m), int(nrow), *(x.ctypes.data for x in arrs),
+                                        PRECISIONS[precision]), "SharedMatrix")
         self._h = h
-        self.m, self.nrow = int(m), int(nrow)
+        self.m, self.nrow, self.precision = int(m), int(nrow), precision
 
     def solve(self, rhs, x=None, lines: Lines | None = None, stream=None):
         """x <- M^{-1} rhs on every line (CUDA float64 tensors; x defaults to
@@ -152,3 +158,48 @@ def heat3d_blocks(nblk: int, sigma: float, is_first: bool = True, is_last: bool 
         Cc[:, :, -1] = 0.0
     # element (i, j) of row q at q + nblk*(i + m*j): axis order (j, i, q) in C order
     return tuple(np.ascontiguousarray(x.transpose(1, 0, 2)).reshape(-1) for x in (A, B, Cc))
+
+
+def sweep_field(n: int, axis: int, precision: str = "ff", sweeps: int = 3, halo: int = 2, sigma: float = 0.05,
+                device: str = "cuda:0") -> float:
+    """Solve the heat3d lines (m = 2, n/2 blocks) along `axis` of a random
+    (n + 2*halo)^3 field in place, `sweeps` times; returns ms per sweep
+    (CUDA events, after one untimed sweep)."""
+    import torch
+
+    if n % 2:
+        raise ValueError("n must be even (blocks of two points)")
+    field = torch.rand((n + 2 * halo,) * 3, dtype=torch.float64, device=device)
+    interior = field[halo:-halo, halo:-halo, halo:-halo]
+    st = interior.stride()
+    outer, inner = [x for x in range(3) if x != axis]
+    lines = Lines(n, n, st[inner], st[outer], 2 * st[axis], st[axis])
+    a, b, c = heat3d_blocks(n // 2, sigma)
+    with SharedMatrix(2, n // 2, a, b, c, precision=precision) as sm:
+        sm.solve(interior, interior, lines)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(sweeps):
+            sm.solve(interior, interior, lines)
+        e1.record()
+        torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / sweeps
+
+
+def main(argv=None) -> None:
+    import argparse
+
+    ap = argparse.ArgumentParser(description="heat3d-style sweeps of shared-matrix lines in a haloed field")
+    ap.add_argument("n", type=int, help="interior points per axis (even)")
+    ap.add_argument("--axis", type=int, default=0, choices=[0, 1, 2], help="0 = slowest (z), 2 = fastest (x)")
+    ap.add_argument("--precision", default="ff", choices=["fp64", "ff"])
+    ap.add_argument("--sweeps", type=int, default=3)
+    args = ap.parse_args(argv)
+    ms = sweep_field(args.n, args.axis, args.precision, args.sweeps)
+    rows = args.n * args.n * (args.n // 2)
+    print(f"n={args.n} axis={args.axis} precision={args.precision}: {ms:.3f} ms/sweep, "
+          f"{rows / ms / 1e6:.2f} G block rows/s")
+
+
+if __name__ == "__main__":
+    main()

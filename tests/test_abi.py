@@ -189,6 +189,19 @@ def test_shared_create_checks_before_the_gpu():
     a, b, c = (np.zeros(nrow * m * m) for _ in range(3))  # B = 0: the first pivot is zero
     with pytest.raises(pbt.SingularBlockError):
         shared.SharedMatrix(m, nrow, a, b, c)
+    with pytest.raises(ValueError):
+        shared.SharedMatrix(m, nrow, a, b, c, precision="fp32_refine")
+    # The C entry refuses other arithmetics itself, and float-float factors
+    # beyond the float range (1/b = 1e40 here), before any device call.
+    lib = shared._lib()
+    h = C.c_void_p()
+    one = np.ones(nrow * m * m)
+    assert lib.pbt_shared_create(C.byref(h), m, nrow, one.ctypes.data, one.ctypes.data, one.ctypes.data,
+                                 N.PBT_PREC_FP32_REFINE) == N.PBT_EUNSUPPORTED
+    tiny, zero = np.full(2, 1e-40), np.zeros(2)
+    assert lib.pbt_shared_create(C.byref(h), 1, 2, zero.ctypes.data, tiny.ctypes.data, tiny.ctypes.data,
+                                 N.PBT_PREC_FF) == N.PBT_EINVAL
+    assert not h.value
 
 
 def test_heat3d_blocks_match_reference_stencil():
