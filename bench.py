@@ -29,7 +29,9 @@ N = 128, P = 4 timed with L2 flushed, and the pencil batch as periodic lines,
 P = 2), `mixed_precision`, `adjoint`,
 `uneven_batch`, `shared_lines` (one heat3d ADI step, three sweeps of
 shared-matrix lines in place in a 516^3 haloed field, against the general
-solver with pack/unpack), `clocks` (nvidia-smi sampled during the timed
+solver with pack/unpack), `strided_lines` (the y sweep of a 256^3 euler3d
+layout field at m = 5 solved in the application's arrays against
+transpose-solve-transpose), `clocks` (nvidia-smi sampled during the timed
 region).
 `--sections` limits the extra sections (e.g. `--sections main`).
 
@@ -165,6 +167,64 @@ def run_shared(dev) -> dict:
     out["general_ff_pack_solve_unpack_ms_per_sweep"] = gen * 1e3
     out["speedup_ff_vs_general_ff"] = gen / (out["ff"]["ms_per_adi_step"] / 3e3)
     del field, interior, rep, d
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_lines(dev) -> dict:
+    """Strided lines (pbt_solve_noncyclic_lines): the y sweep of an euler3d
+    layout field, U(n1,n2,n3,m) and trA(n1,n2,n3,m,m) with n = 256, m = 5
+    (the headline's 65536 lines of 256 rows), solved in the application's
+    arrays, against the reference application's route: transpose A, B, C, D
+    into the solver layout, solve, transpose D back (PyTorch copies)."""
+    import torch
+
+    import pascal_btdma_gb300 as pbt
+    from pascal_btdma_gb300 import synth
+
+    n, m = 256, 5
+    nsys, nrow = n * n, n
+    w = synth.dominant(m, nsys, nrow, seed=SEED, delta=DELTA)
+    # packed [e, row = j, s_out = k, s_in = i] -> application [e, k, j, i]
+    app = [torch.from_numpy(x).to(dev).view(-1, n, n, n).transpose(1, 2).contiguous() for x in w.arrays]
+    lines = pbt.Lines(n, n, 1, n * n, n, n * n * n)
+    out = {"field": [n, n, n], "m": m, "sweep": "y (lines over i, k; rows along j)", "lines": nsys, "rows": nrow}
+    steps = 5
+    for prec in ("ff", "fp64"):
+        d0 = app[3].clone()
+        with pbt.BtdmaGpuPlan() as pl:
+            pl.create(m, nsys, nrow, 1, precision=prec)
+            bufs = [d0.clone() for _ in range(steps + 1)]
+            pbt.solve_noncyclic_lines(pl, *app[:3], bufs[-1], lines)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for k in range(steps):
+                pbt.solve_noncyclic_lines(pl, *app[:3], bufs[k], lines)
+            e1.record()
+            torch.cuda.synchronize()
+            t_lines = e0.elapsed_time(e1) / steps
+            packed = [torch.empty(x.numel(), dtype=torch.float64, device=dev) for x in app]
+
+            def transposed_sweep(dk):
+                for src, dst in zip(app[:3] + [dk], packed):
+                    dst.view(-1, n, n, n).copy_(src.transpose(1, 2))
+                pbt.solve_noncyclic(pl, *packed, m, nsys, nrow)
+                dk.copy_(packed[3].view(-1, n, n, n).transpose(1, 2))
+
+            transposed_sweep(bufs[-1])
+            torch.cuda.synchronize()
+            e0.record()
+            for k in range(steps):
+                transposed_sweep(bufs[k])
+            e1.record()
+            torch.cuda.synchronize()
+            t_tr = e0.elapsed_time(e1) / steps
+            del packed
+        out[prec] = {"lines_ms": t_lines, "transpose_solve_transpose_ms": t_tr, "speedup": t_tr / t_lines,
+                     "block_rows_per_s": nsys * nrow / (t_lines / 1e3)}
+        del bufs, d0
+    del app
     torch.cuda.empty_cache()
     return out
 
@@ -694,6 +754,7 @@ def run_ours(args):
         torch.cuda.empty_cache()
     uneven = run_uneven(dev) if "uneven" in args.sections else {}
     shared_lines = run_shared(dev) if "shared" in args.sections else {}
+    strided_lines = run_lines(dev) if "lines" in args.sections else {}
 
     result = {
         "metric": METRIC,
@@ -735,6 +796,7 @@ def run_ours(args):
         "adjoint": adjoint,
         "uneven_batch": uneven,
         "shared_lines": shared_lines,
+        "strided_lines": strided_lines,
     }
     if rank == 0:
         if "cpu" in args.sections:
@@ -795,11 +857,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--sections", default="all",
                     help="comma list of extra sections to run beside the headline: variants, mixed, adjoint, "
-                         "uneven, shared, cpu; 'all' (default) or 'main' (headline only)")
+                         "uneven, shared, lines, cpu; 'all' (default) or 'main' (headline only)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    known = {"variants", "mixed", "adjoint", "uneven", "shared", "cpu"}
+    known = {"variants", "mixed", "adjoint", "uneven", "shared", "lines", "cpu"}
     if args.sections == "all":
         args.sections = known
     elif args.sections == "main":

@@ -160,6 +160,41 @@ int pbt_solve_noncyclic_profiled(pbt_plan* plan, double* a, double* b, double* c
 int pbt_solve_cyclic(pbt_plan* plan, double* a, double* b, double* c, double* d,
                      int m, int nsys, int nrow, void* stream);
 
+/* Lines addressed by strides: line s = s_in + nsys_inner * s_out, block row
+ * q, element e of the row's block (e = i + m*j for A, B, C; e = i for D) at
+ * element offset
+ *   s_in*stride_inner + s_out*stride_outer + q*row_stride + e*elem_stride.
+ * The reference GPU layout is {nsys, 1, 1, 0, nsys, nsys*nrow}.  Threads go
+ * to consecutive s_in: stride_inner = 1 keeps the loads coalesced. */
+typedef struct pbt_lines {
+    int nsys_inner;         /* lines along the fast index (threads) */
+    int nsys_outer;         /* lines along the slow index */
+    long long stride_inner; /* element offset between consecutive inner lines */
+    long long stride_outer; /* element offset between consecutive outer lines */
+    long long row_stride;   /* element offset between block rows of a line */
+    long long elem_stride;  /* element offset between the elements of a row */
+} pbt_lines;
+
+/* Non-cyclic solve of lines that live in the caller's own arrays, addressed
+ * by `lines` (the same strides for A, B, C and D).
+ *
+ * No single counterpart in the reference API: it removes the transposes that
+ * the reference's applications run around each solve to bring their arrays
+ * into the solver layout, e.g. euler3d's transpose_jk / transpose_ik kernels
+ * and their 5-D block versions (Fortran_Original/examples/euler3d/
+ * euler3d_mpi_gpu.f90:931-1017) around btdma_many_mpi_gpu_v2: with
+ * U(n1,n2,n3,m) and trA(n1,n2,n3,m,m) the y sweep is
+ *   {n1, n3, 1, n1*n2, n1, n1*n2*n3}.
+ * The plan must be a single-segment, non-cyclic FP64 or PBT_PREC_FF plan
+ * (nseg = 1, no PBT_FLAG_REFERENCE_METHOD / PBT_FLAG_CPU_LAYOUT) with
+ * nsys = nsys_inner * nsys_outer; otherwise PBT_EUNSUPPORTED / PBT_EINVAL.
+ * A PBT_FLAG_INPLACE plan writes C' into C, as the reference does; any other
+ * plan keeps its factors in its workspace, addressed with the same strides,
+ * so the lines must then fit in nsys*nrow*m*m elements (a dense layout, as
+ * euler3d's), else PBT_EUNSUPPORTED.  Always the direct-load kernel. */
+int pbt_solve_noncyclic_lines(pbt_plan* plan, double* a, double* b, double* c, double* d,
+                              const pbt_lines* lines, void* stream);
+
 /* Solve without a plan and without allocating device memory.
  *
  * No counterpart in the reference.  It exists for callers that cannot call

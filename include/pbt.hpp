@@ -145,6 +145,13 @@ inline void solve_cyclic(BtdmaGpuPlan& plan, double* a, double* b, double* c, do
     check(pbt_solve_cyclic(plan.get(), a, b, c, d, m, nsys, nrow, stream), "solve_cyclic");
 }
 
+// Lines in the caller's own arrays (pbt_solve_noncyclic_lines; no reference
+// counterpart: it replaces the transposes around each solve).
+inline void solve_noncyclic_lines(BtdmaGpuPlan& plan, double* a, double* b, double* c, double* d,
+                                  const pbt_lines& lines, void* stream = nullptr) {
+    check(pbt_solve_noncyclic_lines(plan.get(), a, b, c, d, &lines, stream), "solve_noncyclic_lines");
+}
+
 inline std::pair<int, int> partition_1d(int start, int end, int nparts, int part) {
     int first = 0, last = -1;
     pbt_partition_1d(start, end, nparts, part, &first, &last);

@@ -38,15 +38,8 @@ extern "C" {
 
 typedef struct pbt_shared pbt_shared;
 
-typedef struct pbt_lines {
-    int nsys_inner;         /* lines along the fast index (threads) */
-    int nsys_outer;         /* lines along the slow index */
-    long long stride_inner; /* element offset between consecutive inner lines */
-    long long stride_outer; /* element offset between consecutive outer lines */
-    long long row_stride;   /* element offset between block rows of a line */
-    long long elem_stride;  /* element offset between the m unknowns of a row */
-} pbt_lines;
-
+/* pbt_lines (pbt.h) gives where the m unknowns of each block row of each
+ * line live in rhs and x. */
 /* Factorise the matrix every line shares: a, b, c are HOST arrays of one
  * system, nrow*m*m doubles each, element (i, j) of row q at q + nrow*(i + m*j)
  * (the reference layout with nsys = 1); A_0 and C_{nrow-1} are ignored.  The

@@ -283,6 +283,27 @@ def solve_cyclic(plan, a, b, c, d, m, nsys, nrow, stream=None) -> None:
     _solve(N.lib().pbt_solve_cyclic, "solve_cyclic", plan, a, b, c, d, m, nsys, nrow, stream)
 
 
+def solve_noncyclic_lines(plan, a, b, c, d, lines, stream=None) -> None:
+    """Solve lines that live in the caller's own arrays, addressed by
+    ``lines`` (a ``Lines``; the same strides for A, B, C and D, which may be
+    strided views): D <- x.  Replaces the transposes the reference's
+    applications run around each solve (euler3d_mpi_gpu.f90:931-1017).  The
+    plan: single segment, non-cyclic, FP64 or "ff", ``nsys`` lines; an
+    ``inplace`` plan writes C' into C, any other needs a dense layout."""
+    if not isinstance(plan, BtdmaGpuPlan) or not plan.created:
+        raise RuntimeError("solve_noncyclic_lines called with an uncreated BtdmaGpuPlan")
+    import torch
+
+    arrays = (a, b, c, d)
+    for x in arrays:
+        if not (hasattr(x, "data_ptr") and x.is_cuda and x.dtype == torch.float64):
+            raise ValueError("arrays must be float64 CUDA tensors (strided views allowed)")
+    lc = lines.c() if hasattr(lines, "c") else lines
+    s = _stream(stream, arrays)
+    _raise(N.lib().pbt_solve_noncyclic_lines(plan.handle, *(C.c_void_p(x.data_ptr()) for x in arrays), C.byref(lc),
+                                             C.c_void_p(s)), "solve_noncyclic_lines")
+
+
 def partition_1d(start: int, end: int, nprocs: int, rank: int) -> tuple[int, int]:
     """(first, last) of part ``rank`` of [start, end] (pascal_btdma_cuda.cu:921-930)."""
     f, l = C.c_int(), C.c_int()
@@ -368,3 +389,5 @@ class _LazySolve:
 
 
 BlockTridiagonalSolve = _LazySolve()
+
+from .shared import Lines  # noqa: E402  (shared imports _raise from this module)

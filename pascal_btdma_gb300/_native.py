@@ -62,6 +62,14 @@ class Timings(C.Structure):
     ]
 
 
+class Lines(C.Structure):
+    """pbt_lines: line s = s_in + nsys_inner*s_out, row q, element e at
+    s_in*stride_inner + s_out*stride_outer + q*row_stride + e*elem_stride."""
+
+    _fields_ = [("nsys_inner", C.c_int), ("nsys_outer", C.c_int), ("stride_inner", C.c_longlong),
+                ("stride_outer", C.c_longlong), ("row_stride", C.c_longlong), ("elem_stride", C.c_longlong)]
+
+
 # Every function include/pbt.h declares, with its ctypes signature.
 _P = C.c_void_p
 _D = C.c_void_p  # device pointer to double
@@ -76,6 +84,7 @@ SIGNATURES = {
         [_P, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, C.POINTER(Timings), _P],
     ),
     "pbt_solve_cyclic": (C.c_int, [_P, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, _P]),
+    "pbt_solve_noncyclic_lines": (C.c_int, [_P, _D, _D, _D, _D, C.POINTER(Lines), _P]),
     "pbt_adjoint_noncyclic": (
         C.c_int,
         [_P, _D, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int, _P],

@@ -183,6 +183,13 @@ cudaError_t run_accumulate(int m, const pbt::SolveArgs& g, double* X, const doub
 
 PBT_DISPATCH(run_thomas, launch_thomas)
 
+cudaError_t run_thomas_lines(int arith, int m, const pbt::SolveArgs& g, const pbt::LineStrides& ls) {
+    if (arith == kFF) {
+        PBT_DISPATCH_PLAIN_M2(pbt::FF, launch_thomas_lines, g, ls)
+    }
+    PBT_DISPATCH_PLAIN_M2(pbt::F64, launch_thomas_lines, g, ls)
+}
+
 #define PBT_DISPATCH_STAGED_M(NUM)                                         \
     switch (m) {                                                           \
         case 1: return pbt::launch_thomas_staged<NUM, 1>(g, maps);         \
@@ -751,6 +758,41 @@ int pbt_solve_noncyclic_profiled(pbt_plan* p, double* a, double* b, double* c, d
 int pbt_solve_cyclic(pbt_plan* p, double* a, double* b, double* c, double* d, int m, int nsys, int nrow,
                      void* stream) {
     return solve_impl(p, a, b, c, d, m, nsys, nrow, true, nullptr, stream);
+}
+
+int pbt_solve_noncyclic_lines(pbt_plan* p, double* a, double* b, double* c, double* d, const pbt_lines* L,
+                              void* stream) {
+    int rc = check_plan(p);
+    if (rc) return rc;
+    const pbt_plan_desc& ds = p->desc;
+    if (!a || !b || !c || !d || !L) return fail(PBT_EINVAL, "solve_lines: null argument");
+    if (!p->thomas || (ds.flags & PBT_FLAG_CPU_LAYOUT) || ds.precision == PBT_PREC_FP32_REFINE)
+        return fail(PBT_EUNSUPPORTED,
+                    "solve_lines: needs a single-segment, non-cyclic FP64 or float-float plan in the GPU layout");
+    if (L->nsys_inner <= 0 || L->nsys_outer <= 0 || (long long)L->nsys_inner * L->nsys_outer != ds.nsys) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "solve_lines: %d x %d lines for a plan of %d systems", L->nsys_inner,
+                      L->nsys_outer, ds.nsys);
+        return fail(PBT_EINVAL, buf);
+    }
+    if (L->stride_inner < 0 || L->stride_outer < 0 || L->row_stride < 0 || L->elem_stride < 0)
+        return fail(PBT_EINVAL, "solve_lines: negative stride");
+    const long long mm = (long long)ds.m * ds.m;
+    // One past the last element a block array is addressed at.
+    const long long extent = (long long)(L->nsys_inner - 1) * L->stride_inner +
+                             (long long)(L->nsys_outer - 1) * L->stride_outer +
+                             (long long)(ds.nrow - 1) * L->row_stride + (mm - 1) * L->elem_stride + 1;
+    const bool inplace = (ds.flags & PBT_FLAG_INPLACE) != 0;
+    if (!inplace && extent > mm * ds.nsys * ds.nrow)
+        return fail(PBT_EUNSUPPORTED,
+                    "solve_lines: the lines span more than the plan's factor workspace (nsys*nrow*m*m); "
+                    "use a PBT_FLAG_INPLACE plan for a non-dense layout");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    p->last_stream = s;
+    const pbt::LineStrides ls{L->nsys_inner, L->stride_inner, L->stride_outer, L->row_stride, L->elem_stride};
+    cudaError_t e = run_thomas_lines(arith_of(ds.precision), ds.m, make_args(p, a, b, c, d, s, ds.nsys), ls);
+    if (e != cudaSuccess) return cuda_fail(e, "block Thomas launch (strided lines)");
+    return PBT_OK;
 }
 
 int pbt_plan_status(pbt_plan* p, long long* nsingular) {

@@ -17,6 +17,7 @@
 
 namespace pbt {
 template cudaError_t launch_thomas<PBT_NUM, PBT_M>(const SolveArgs&);
+template cudaError_t launch_thomas_lines<PBT_NUM, PBT_M>(const SolveArgs&, const LineStrides&);
 #if PBT_M <= 6
 template cudaError_t launch_thomas_staged<PBT_NUM, PBT_M>(const SolveArgs&, const ThomasMaps&);
 #endif

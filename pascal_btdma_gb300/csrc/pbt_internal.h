@@ -35,6 +35,14 @@ struct SolveArgs {
     cudaStream_t stream;
 };
 
+// Strided lines (pbt_solve_noncyclic_lines): line sys at
+// (sys % lin)*in + (sys / lin)*out, rows `row` apart, elements `elem` apart,
+// in A, B, C, D and the factor array alike.
+struct LineStrides {
+    int lin;
+    long long in, out, row, elem;
+};
+
 // The arithmetics of pbt_num.cuh.
 struct F64;
 struct FF;
@@ -57,6 +65,7 @@ constexpr unsigned long long kStallMark = 1ull << 48;
 // Kernel launchers, explicitly instantiated per arithmetic and block size M
 // (1..PBT_MAX_BLOCK) in pbt_inst.cu.  Each returns cudaGetLastError().
 template <class Num, int M> cudaError_t launch_thomas(const SolveArgs& g);
+template <class Num, int M> cudaError_t launch_thomas_lines(const SolveArgs& g, const LineStrides& ls);
 template <class Num, int M> cudaError_t launch_thomas_staged(const SolveArgs& g, const ThomasMaps& maps);
 template <class Num, int M> cudaError_t launch_modi(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced(const SolveArgs& g);

@@ -33,6 +33,8 @@
 // caller's A and C are converted to FP64 so those arrays stay valid doubles.
 #pragma once
 
+#include <type_traits>
+
 #include "pbt_util.cuh"
 #include "pbt_internal.h"
 #include "pbt_num.cuh"
@@ -653,6 +655,28 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
     } else {
         thomas_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
                             (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
+    }
+    if (bad) atomicAdd(g.status, 1ull);
+}
+
+// The same solve for lines addressed by strides (pbt_solve_noncyclic_lines).
+// Kept apart from k_thomas, whose code generation at m = 5 proved sensitive:
+// folding the strides into it (chosen at run time or by a template parameter,
+// with the strides carried in SolveArgs) made the reference-layout solve ~5 %
+// slower.
+template <class Num, int M>
+__global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_lines(const SolveArgs g, const LineStrides ls) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    bool bad = false;
+    const size_t o = (size_t)(sys % ls.lin) * (size_t)ls.in + (size_t)(sys / ls.lin) * (size_t)ls.out;
+    if constexpr (thomas_uses_lu<M>()) {
+        extern __shared__ double thomas_cps[];
+        thomas_body_lu<Num, M>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, thomas_cps + threadIdx.x, blockDim.x,
+                               (size_t)ls.elem, (size_t)ls.row, g.nrow, g.factors_raw != 0, bad);
+    } else {
+        thomas_body<Num, M>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, (size_t)ls.elem, (size_t)ls.row, g.nrow,
+                            g.factors_raw != 0, bad);
     }
     if (bad) atomicAdd(g.status, 1ull);
 }
@@ -1451,6 +1475,17 @@ cudaError_t launch_thomas(const SolveArgs& g) {
     const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * (M * M + M) * sizeof(double) : 0;
     k_thomas<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g);
     return cudaGetLastError();
+}
+template <class Num, int M>
+cudaError_t launch_thomas_lines(const SolveArgs& g, const LineStrides& ls) {
+    if constexpr (std::is_same<Num, F32>::value) {
+        return cudaErrorInvalidValue;  // FP64 and float-float plans only
+    } else {
+        const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
+        const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * (M * M + M) * sizeof(double) : 0;
+        k_thomas_lines<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g, ls);
+        return cudaGetLastError();
+    }
 }
 template <class Num, int M>
 cudaError_t launch_modi(const SolveArgs& g) {

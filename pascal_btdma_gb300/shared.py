@@ -20,10 +20,7 @@ from . import _native as N
 from . import _raise
 
 
-class _LinesC(C.Structure):
-    _fields_ = [("nsys_inner", C.c_int), ("nsys_outer", C.c_int), ("stride_inner", C.c_longlong),
-                ("stride_outer", C.c_longlong), ("row_stride", C.c_longlong), ("elem_stride", C.c_longlong)]
-
+_LinesC = N.Lines
 
 _P = C.c_void_p
 SHARED_SIGNATURES = {
