@@ -180,6 +180,9 @@ cudaError_t run_residual(int m, const pbt::SolveArgs& g, const double* X, double
 cudaError_t run_accumulate(int m, const pbt::SolveArgs& g, double* X, const double* E, unsigned* stat) {
     PBT_DISPATCH_PLAIN_M(launch_accumulate, g, X, E, stat)
 }
+cudaError_t run_refine_step(int m, const pbt::SolveArgs& g, const pbt::RefineArgs& ra) {
+    PBT_DISPATCH_PLAIN_M(launch_refine_step, g, ra)
+}
 
 PBT_DISPATCH(run_thomas, launch_thomas)
 
@@ -247,6 +250,21 @@ bool encode_columns(CUtensorMap* tm, const double* base, int nsys, int nrow, int
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The FP32 staged solve keeps C' as floats: the same tensor over 4-byte
+// elements (strides multiples of 16 bytes: nsys a multiple of 4).
+bool encode_columns_f32(CUtensorMap* tm, const double* base, int nsys, int nrow, int planes, int m) {
+    const PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+    if (fn == nullptr || base == nullptr || (reinterpret_cast<std::uintptr_t>(base) & 15u) != 0 || (nsys & 3))
+        return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)nsys, (cuuint64_t)nrow, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)nsys * 4u, (cuuint64_t)nsys * (cuuint64_t)nrow * 4u};
+    const cuuint32_t box[3] = {32u, 1u, (cuuint32_t)m};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    return fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<double*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Launch the single-segment block Thomas solve, with TMA-staged loads
 // (k_thomas_staged) or direct loads (k_thomas); both give the same bits.
 // The default follows GB300 measurements (float-float unless noted, N = 256
@@ -265,7 +283,7 @@ bool prefer_staged(int arith, int m, int nsys, int sms) {
     return (m == 5 || m == 6) && small;
 }
 
-cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveArgs& g) {
+cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveArgs& g, bool* ran_staged = nullptr) {
     const pbt_plan_desc& ds = p->desc;
     bool staged;
     if (ds.flags & PBT_FLAG_DIRECT_LOADS)
@@ -279,9 +297,13 @@ cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveA
         const int mm = m * m;
         if (encode_columns(&maps.a, g.a, g.nsys, g.nrow, mm, m) && encode_columns(&maps.b, g.b, g.nsys, g.nrow, mm, m) &&
             encode_columns(&maps.c, g.c, g.nsys, g.nrow, mm, m) && encode_columns(&maps.d, g.d, g.nsys, g.nrow, m, m) &&
-            encode_columns(&maps.w, g.cw, g.nsys, g.nrow, mm, m))
+            (arith == kF32 ? encode_columns_f32(&maps.w, g.cw, g.nsys, g.nrow, mm, m)
+                           : encode_columns(&maps.w, g.cw, g.nsys, g.nrow, mm, m))) {
+            if (ran_staged) *ran_staged = true;
             return run_thomas_staged(arith, m, g, maps);
+        }
     }
+    if (ran_staged) *ran_staged = false;
     return run_thomas(arith, m, g);
 }
 
@@ -454,36 +476,61 @@ struct EventSet {
     }
 };
 
-// The refined solve: x = 0, r = d; repeat { solve M e = r with FP32
-// arithmetic (same kernels, F32); x += e; stop when the estimated remaining
-// error, c_k^2 / c_{k-1} with c_k = max over systems of max|e|/max|x| (and
-// c_0 = 1), is <= tol, or after max_iter FP32 solves; r = d - M x in FP64 }.
-// Synchronises the stream once per FP32 solve to test convergence.
+// The refined solve: keep the right-hand side d in p->rx; x_1 = the FP32
+// solve of M x = d (same kernels, F32 arithmetic, in place in D); then repeat
+// { r = d - M x in FP64; solve M e = r in FP32; x += e } until the estimated
+// remaining error, c_k^2 / c_{k-1} with c_k = max over systems of
+// max|e|/max|x| (c_1 = 1: the first solve is a correction of size 1), is <=
+// tol, or after max_iter FP32 solves.  x lives in D throughout, so the
+// result needs no copy.  Synchronises the stream once per correction to test
+// convergence.
 int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaStream_t s) {
     const pbt_plan_desc& ds = p->desc;
     const int m = ds.m;
     const size_t nv = (size_t)ds.nsys * ds.nrow * ds.m;
-    cudaError_t e = cudaMemcpyAsync(p->re_, d, nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p->rx, 0, nv * sizeof(double), s);
-    if (e != cudaSuccess) return cuda_fail(e, "refined solve: set-up copies");
     p->last_iters = 0;
     p->last_correction = 0.0;
-    const pbt::SolveArgs g64 = make_args(p, a, b, c, d, s, ds.nsys);
+    auto fp32_solve = [&](double* rhs) -> cudaError_t {
+        if (p->thomas) return thomas_launch(p, kF32, m, make_args(p, a, b, c, rhs, s, ds.nsys));
+        pbt::SolveArgs g = make_args(p, a, b, c, rhs, s, ds.nsys * ds.nseg);
+        cudaError_t e = run_modi(kF32, m, g);
+        if (e == cudaSuccess) e = run_reduced(kF32, m, make_args(p, a, b, c, rhs, s, ds.nsys));
+        if (e == cudaSuccess) e = run_update(kF32, m, g);
+        return e;
+    };
+    double* const rhs = p->rx;
+    cudaError_t e = cudaMemcpyAsync(rhs, d, nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "refined solve: set-up copy");
+    // A single-segment plan whose first pass ran the staged kernel has the
+    // FP32 factors (in p->aw); its corrections are then one k_refine_step
+    // each.  Otherwise: residual, FP32 solve, accumulate.
+    bool staged = false;
+    if (p->thomas)
+        e = thomas_launch(p, kF32, m, make_args(p, a, b, c, d, s, ds.nsys), &staged);
+    else
+        e = fp32_solve(d);
+    if (e != cudaSuccess) return cuda_fail(e, "refined solve: FP32 solve launch");
+    const bool fused = staged && p->aw != nullptr && m <= pbt::kStagedMaxBlock;
+    p->last_iters = 1;
+    p->last_correction = 1.0;
+    const pbt::SolveArgs g64 = make_args(p, a, b, c, rhs, s, ds.nsys);
     double prev_ratio = 1.0;
-    for (int it = 0; it < ds.max_iter; ++it) {
-        if (p->thomas) {
-            e = thomas_launch(p, kF32, m, make_args(p, a, b, c, p->re_, s, ds.nsys));
-        } else {
-            pbt::SolveArgs g = make_args(p, a, b, c, p->re_, s, ds.nsys * ds.nseg);
-            e = run_modi(kF32, m, g);
-            if (e == cudaSuccess) e = run_reduced(kF32, m, make_args(p, a, b, c, p->re_, s, ds.nsys));
-            if (e == cudaSuccess) e = run_update(kF32, m, g);
-        }
-        if (e != cudaSuccess) return cuda_fail(e, "refined solve: FP32 correction launch");
+    for (int it = 1; it < ds.max_iter; ++it) {
         if ((e = cudaMemsetAsync(p->rstat, 0, sizeof(unsigned), s)) != cudaSuccess)
             return cuda_fail(e, "refined solve: statistic reset");
-        if ((e = run_accumulate(m, g64, p->rx, p->re_, p->rstat)) != cudaSuccess)
-            return cuda_fail(e, "refined solve: accumulate launch");
+        if (fused) {
+            const pbt::RefineArgs ra{reinterpret_cast<const float*>(p->aw), reinterpret_cast<float*>(p->re_), d,
+                                     p->rstat};
+            if ((e = run_refine_step(m, g64, ra)) != cudaSuccess)
+                return cuda_fail(e, "refined solve: correction launch");
+        } else {
+            if ((e = run_residual(m, g64, d, p->re_)) != cudaSuccess)
+                return cuda_fail(e, "refined solve: residual launch");
+            if ((e = fp32_solve(p->re_)) != cudaSuccess)
+                return cuda_fail(e, "refined solve: FP32 correction launch");
+            if ((e = run_accumulate(m, g64, d, p->re_, p->rstat)) != cudaSuccess)
+                return cuda_fail(e, "refined solve: accumulate launch");
+        }
         unsigned bits = 0;
         if ((e = cudaMemcpyAsync(&bits, p->rstat, sizeof bits, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess)
@@ -493,16 +540,11 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
         p->last_iters = it + 1;
         p->last_correction = ratio;
         // Stop when the estimated error left after this correction,
-        // ratio * rho with the contraction rho = ratio / previous ratio
-        // (the first solve counts as a correction of size 1), is below tol.
-        if (it > 0 && (double)ratio * ((double)ratio / prev_ratio) <= ds.tol) break;
+        // ratio * rho with the contraction rho = ratio / previous ratio, is
+        // below tol.
+        if ((double)ratio * ((double)ratio / prev_ratio) <= ds.tol) break;
         prev_ratio = ratio > 0.f ? (double)ratio : 1e-300;
-        if (it + 1 == ds.max_iter) break;
-        if ((e = run_residual(m, g64, p->rx, p->re_)) != cudaSuccess)
-            return cuda_fail(e, "refined solve: residual launch");
     }
-    e = cudaMemcpyAsync(d, p->rx, nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return cuda_fail(e, "refined solve: result copy");
     return PBT_OK;
 }
 
@@ -667,7 +709,13 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
     const size_t rrows = (size_t)d.nsys * 2 * d.nseg;
     if (!inplace) {
         if ((rc = alloc(p, &p->cw, mm * rows))) goto fail_out;
+        // aw: A' for the two-stage method; for a single-segment refined plan,
+        // the FP32 factors its first pass keeps: per row and warp of 32
+        // systems, m*m + 1 runs of 32 floats.
+        const bool keep_lu = p->thomas && d.precision == PBT_PREC_FP32_REFINE && d.m <= pbt::kStagedMaxBlock;
+        const size_t lu_doubles = (size_t)d.nrow * ((d.nsys + 31) / 32) * 16 * (mm + 1);
         if (!p->thomas && (rc = alloc(p, &p->aw, mm * rows))) goto fail_out;
+        if (keep_lu && (rc = alloc(p, &p->aw, lu_doubles))) goto fail_out;
     }
     if (!p->thomas) {
         if ((rc = alloc(p, &p->ra, mm * rrows))) goto fail_out;

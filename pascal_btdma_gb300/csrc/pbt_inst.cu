@@ -31,5 +31,6 @@ template cudaError_t launch_transpose_blocks<PBT_M>(const SolveArgs&, double*, d
 template cudaError_t launch_gradients<PBT_M>(const SolveArgs&, const AdjointArgs&);
 template cudaError_t launch_residual<PBT_M>(const SolveArgs&, const double*, double*);
 template cudaError_t launch_accumulate<PBT_M>(const SolveArgs&, double*, const double*, unsigned*);
+template cudaError_t launch_refine_step<PBT_M>(const SolveArgs&, const RefineArgs&);
 #endif
 }  // namespace pbt

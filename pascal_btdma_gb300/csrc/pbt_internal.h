@@ -86,6 +86,19 @@ template <int M> cudaError_t launch_gradients(const SolveArgs& g, const AdjointA
 template <int M> cudaError_t launch_residual(const SolveArgs& g, const double* X, double* E);
 template <int M> cudaError_t launch_accumulate(const SolveArgs& g, double* X, const double* E, unsigned* stat);
 
+// One correction of the refined solve with stored FP32 factors
+// (k_refine_step): lu = the factors the staged FP32 pass kept (per row and
+// warp of 32 systems, m*m + 1 runs of 32 floats), y = float scratch of
+// nsys*nrow*m, x = the FP64 solution (updated), stat = the convergence
+// statistic.
+struct RefineArgs {
+    const float* lu;
+    float* y;
+    double* x;
+    unsigned* stat;
+};
+template <int M> cudaError_t launch_refine_step(const SolveArgs& g, const RefineArgs& ra);
+
 // Layout conversion for PBT_FLAG_CPU_LAYOUT plans (pbt_layout.cu): E elements
 // per (system, row); dir 0: CPU layout src -> GPU layout dst, 1: back.
 cudaError_t launch_layout(const double* src, double* dst, int E, int nsys, int nrow, int dir, cudaStream_t s);

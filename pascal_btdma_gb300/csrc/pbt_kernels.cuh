@@ -1395,73 +1395,215 @@ PBT_UNROLL
 //                 (A_0 and C_{N-1} not read, as in the non-cyclic solve).
 //   k_accumulate: X += E, and the largest max|E| / max|X| over the systems
 //                 into *stat (as ordered float bits) for the convergence test.
+// Both run one thread per (system, block row i): a CTA is M warps over the
+// same 32 systems (warp i = row i), so the FP64 pipe and the memory system
+// see M times the threads of one per system; the M warps read the same x
+// values, which the first of them brings into L1.
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(128) k_residual64(const SolveArgs g, const double* __restrict__ X,
-                                                   double* __restrict__ E) {
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * M, 4) k_residual64(const SolveArgs g, const double* __restrict__ X,
+                                                       double* __restrict__ E) {
+    const int i = threadIdx.y;
+    const int sys = blockIdx.x * 32 + threadIdx.x;
     if (sys >= g.nsys) return;
     const int N = g.nrow;
     const size_t plane0 = (size_t)g.nsys * N;
     const size_t rs = (size_t)g.nsys;
     double xm[M], x0[M], xp[M];
 PBT_UNROLL
-    for (int i = 0; i < M; ++i) {
-        xm[i] = 0.0;
-        x0[i] = X[sys + (size_t)i * plane0];
+    for (int k = 0; k < M; ++k) {
+        xm[k] = 0.0;
+        x0[k] = X[sys + (size_t)k * plane0];
     }
     for (int q = 0; q < N; ++q) {
         const size_t o = (size_t)q * rs + sys;
         const size_t plane = opaque(plane0);
         const bool has_next = (q + 1 < N);
 PBT_UNROLL
-        for (int i = 0; i < M; ++i) xp[i] = has_next ? X[o + rs + (size_t)i * plane] : 0.0;
+        for (int k = 0; k < M; ++k) xp[k] = has_next ? X[o + rs + (size_t)k * plane] : 0.0;
+        double t = __ldg(g.d + o + (size_t)i * plane);
 PBT_UNROLL
-        for (int i = 0; i < M; ++i) {
-            double t = __ldg(g.d + o + (size_t)i * plane);
+        for (int k = 0; k < M; ++k) t = fma(-__ldg(g.b + o + (size_t)(i + M * k) * plane), x0[k], t);
+        if (q > 0) {
 PBT_UNROLL
-            for (int k = 0; k < M; ++k) t = fma(-__ldg(g.b + o + (size_t)(i + M * k) * plane), x0[k], t);
-            if (q > 0) {
-PBT_UNROLL
-                for (int k = 0; k < M; ++k) t = fma(-__ldg(g.a + o + (size_t)(i + M * k) * plane), xm[k], t);
-            }
-            if (has_next) {
-PBT_UNROLL
-                for (int k = 0; k < M; ++k) t = fma(-__ldg(g.c + o + (size_t)(i + M * k) * plane), xp[k], t);
-            }
-            E[o + (size_t)i * plane] = t;
+            for (int k = 0; k < M; ++k) t = fma(-__ldg(g.a + o + (size_t)(i + M * k) * plane), xm[k], t);
         }
+        if (has_next) {
 PBT_UNROLL
-        for (int i = 0; i < M; ++i) {
-            xm[i] = x0[i];
-            x0[i] = xp[i];
+            for (int k = 0; k < M; ++k) t = fma(-__ldg(g.c + o + (size_t)(i + M * k) * plane), xp[k], t);
+        }
+        E[o + (size_t)i * plane] = t;
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) {
+            xm[k] = x0[k];
+            x0[k] = xp[k];
         }
     }
 }
 
 template <int M>
-__global__ void __launch_bounds__(128) k_accumulate(const SolveArgs g, double* __restrict__ X,
-                                                   const double* __restrict__ E, unsigned* stat) {
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
-    const size_t plane0 = (size_t)g.nsys * g.nrow;
-    const size_t rs = (size_t)g.nsys;
+__global__ void __launch_bounds__(32 * M) k_accumulate(const SolveArgs g, double* __restrict__ X,
+                                                       const double* __restrict__ E, unsigned* stat) {
+    __shared__ double red[2][M][32];
+    const int i = threadIdx.y, lane = threadIdx.x;
+    const int sys = blockIdx.x * 32 + lane;
     double emax = 0.0, xmax = 0.0;
-    for (int q = 0; q < g.nrow; ++q) {
-        const size_t o = (size_t)q * rs + sys;
-PBT_UNROLL
-        for (int i = 0; i < M; ++i) {
-            const double e = E[o + (size_t)i * plane0];
-            const double x = X[o + (size_t)i * plane0] + e;
-            X[o + (size_t)i * plane0] = x;
+    if (sys < g.nsys) {
+        const size_t plane = (size_t)g.nsys * g.nrow;
+        const size_t rs = (size_t)g.nsys;
+        for (int q = 0; q < g.nrow; ++q) {
+            const size_t o = (size_t)q * rs + sys + (size_t)i * plane;
+            const double e = E[o];
+            const double x = X[o] + e;
+            X[o] = x;
             emax = fmax(emax, fabs(e));
             xmax = fmax(xmax, fabs(x));
         }
     }
-    // NaN-safe: a non-finite or undefined ratio reports +Inf.
-    float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
-    if (!(ratio == ratio)) ratio = INFINITY;
-    atomicMax(stat, __float_as_uint(ratio));
+    red[0][i][lane] = emax;
+    red[1][i][lane] = xmax;
+    __syncthreads();
+    if (i == 0) {
+PBT_UNROLL
+        for (int k = 1; k < M; ++k) {
+            emax = fmax(emax, red[0][k][lane]);
+            xmax = fmax(xmax, red[1][k][lane]);
+        }
+        // NaN-safe: a non-finite or undefined ratio reports +Inf.
+        float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
+        if (!(ratio == ratio)) ratio = INFINITY;
+        if (sys < g.nsys) atomicMax(stat, __float_as_uint(ratio));
+    }
+}
+
+// k_refine_step: one whole correction of the refined solve in one pass over
+// A, B, C, when the first FP32 pass kept its factors (the staged kernel,
+// m <= 6).  Forward, row by row: the FP64 residual r_q = d_q - A_q x_{q-1} -
+// B_q x_q - C_q x_{q+1} (the k_residual64 operations in the same order), then
+// t = r_q - A_q y_{q-1} and y_q = R_q^{-1} t in FP32 with the stored LU of R_q
+// (the operations of the FP32 solve, so e is the FP32 solve of r bit for bit;
+// the factors come from ra.lu, tiled by warp as the staged pass wrote them);
+// backward: e_q = y_q - C'_q e_{q+1} with the FP32 pass's C' (floats, as the
+// staged FP32 kernel keeps them), and x_q += e_q
+// with the convergence statistic of k_accumulate.  It reads A, B, C once per
+// correction where the separate residual, FP32 solve and accumulate read them
+// twice and move x and r three more times.
+template <int M>
+__global__ void __launch_bounds__(64) k_refine_step(const SolveArgs g, const RefineArgs ra) {
+    if constexpr (M > kStagedMaxBlock) {
+        return;  // the factors are kept by the staged kernel only (m <= 6)
+    } else {
+        const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+        if (sys >= g.nsys) return;
+        const int N = g.nrow;
+        const size_t plane0 = (size_t)g.nsys * N;
+        const size_t rs = (size_t)g.nsys;
+        const size_t ngroups = ((size_t)g.nsys + 31) / 32;
+        float* Y = ra.y + sys;
+        double* X = ra.x + sys;
+        double xm[M], x0[M], xp[M];
+        float yp[M];
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) {
+            xm[k] = 0.0;
+            x0[k] = X[(size_t)k * plane0];
+            yp[k] = 0.f;
+        }
+        for (int q = 0; q < N; ++q) {
+            const size_t o = (size_t)q * rs;
+            const size_t plane = opaque(plane0);
+            const bool has_next = (q + 1 < N);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) xp[k] = has_next ? X[o + rs + (size_t)k * plane] : 0.0;
+            double r[M];
+            F32::Acc ta[M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                double t = __ldg(g.d + sys + o + (size_t)i * plane);
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) t = fma(-__ldg(g.b + sys + o + (size_t)(i + M * k) * plane), x0[k], t);
+                r[i] = t;
+            }
+            float an[M][M];
+            if (q > 0) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                    for (int k = 0; k < M; ++k) {
+                        const double a = __ldg(g.a + sys + o + (size_t)(i + M * k) * plane);
+                        r[i] = fma(-a, xm[k], r[i]);
+                        an[i][k] = FF::split(a).h;
+                    }
+            }
+            if (has_next) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                    for (int k = 0; k < M; ++k)
+                        r[i] = fma(-__ldg(g.c + sys + o + (size_t)(i + M * k) * plane), xp[k], r[i]);
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) ta[i] = F32::acc(FF::split(r[i]).h);
+            if (q > 0) {
+PBT_UNROLL
+                for (int k = 0; k < M; ++k)
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) F32::msub(ta[i], an[i][k], yp[k]);
+            }
+            LU<F32, M> lu;
+            {
+                const float* lf = ra.lu + ((size_t)q * ngroups + (sys >> 5)) * (size_t)(32 * (M * M + 1)) + (sys & 31);
+PBT_UNROLL
+                for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) lu.f[i][j] = __ldcs(lf + 32 * (i + M * j));
+                lu.piv = __float_as_uint(__ldcs(lf + 32 * M * M));
+            }
+            lu.swaps = 0;
+PBT_UNROLL
+            for (int k = 0; k + 1 < M; ++k)
+                if (__any_sync(__activemask(), ((lu.piv >> (4 * k)) & 15u) != (unsigned)k)) lu.swaps |= 1u << k;
+            lu_solve<F32, M>(lu, ta, yp);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) Y[o + (size_t)i * plane] = yp[i];
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) {
+                xm[k] = x0[k];
+                x0[k] = xp[k];
+            }
+        }
+        double emax = 0.0, xmax = 0.0;
+        float e[M];
+        for (int q = N - 1; q >= 0; --q) {
+            const size_t o = (size_t)q * rs;
+            const size_t plane = opaque(plane0);
+            F32::Acc v[M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) v[i] = F32::acc(Y[o + (size_t)i * plane]);
+            if (q < N - 1) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                    for (int k = 0; k < M; ++k)
+                        F32::msub(v[i], __ldg(reinterpret_cast<const float*>(g.cw) + sys + o + (size_t)(i + M * k) * plane),
+                                  e[k]);
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                e[i] = F32::fin(v[i]);
+                double* px = X + o + (size_t)i * plane;
+                const double ed = FF::widen(e[i]);
+                const double x = *px + ed;
+                *px = x;
+                emax = fmax(emax, fabs(ed));
+                xmax = fmax(xmax, fabs(x));
+            }
+        }
+        // NaN-safe: a non-finite or undefined ratio reports +Inf.
+        float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
+        if (!(ratio == ratio)) ratio = INFINITY;
+        atomicMax(ra.stat, __float_as_uint(ratio));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1523,12 +1665,18 @@ cudaError_t launch_gradients(const SolveArgs& g, const AdjointArgs& adj) {
 }
 template <int M>
 cudaError_t launch_residual(const SolveArgs& g, const double* X, double* E) {
-    k_residual64<M><<<grid_x(g.nsys, 128), 128, 0, g.stream>>>(g, X, E);
+    k_residual64<M><<<grid_x(g.nsys, 32), dim3(32, M), 0, g.stream>>>(g, X, E);
+    return cudaGetLastError();
+}
+template <int M>
+cudaError_t launch_refine_step(const SolveArgs& g, const RefineArgs& ra) {
+    if (M > kStagedMaxBlock) return cudaErrorInvalidValue;
+    k_refine_step<M><<<grid_x(g.nsys, 64), 64, 0, g.stream>>>(g, ra);
     return cudaGetLastError();
 }
 template <int M>
 cudaError_t launch_accumulate(const SolveArgs& g, double* X, const double* E, unsigned* stat) {
-    k_accumulate<M><<<grid_x(g.nsys, 128), 128, 0, g.stream>>>(g, X, E, stat);
+    k_accumulate<M><<<grid_x(g.nsys, 32), dim3(32, M), 0, g.stream>>>(g, X, E, stat);
     return cudaGetLastError();
 }
 template <class Num, int M>

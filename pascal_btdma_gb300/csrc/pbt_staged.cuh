@@ -168,6 +168,11 @@ __device__ __forceinline__ typename Num::T fac_in(const double* p, bool raw) {
 #define PBT_STAGED_MIN_CTAS 16
 #endif
 
+// FP32 (the refined solve's first pass) keeps its factors where the plan
+// provides g.aw.
+template <class Num, int M>
+constexpr bool kKeepLU = std::is_same<Num, F32>::value && !staged_rolled<Num, M>();
+
 template <class Num, int M>
 __global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const __grid_constant__ ThomasMaps maps, const SolveArgs g) {
     using T = typename Num::T;
@@ -202,8 +207,11 @@ __global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const
     int n_cons = 0;
     bool ok = true;
 
+    // FP32 keeps C' as floats (its map is FLOAT32): those items are half a slot.
+    constexpr bool kFloatCW = std::is_same<Num, F32>::value;
     auto issue = [&](int s, const CUtensorMap* map, int row, int z) {
-        mbar_expect_tx(bar_s + 8u * s, kSlotBytes);
+        const unsigned bytes = (kFloatCW && map == &maps.w) ? kSlotBytes / 2 : kSlotBytes;
+        mbar_expect_tx(bar_s + 8u * s, bytes);
         tma_load_3d(ring_s + kSlotBytes * s, map, s0, row, z, bar_s + 8u * s);
     };
     auto take = [&]() -> const double* {
@@ -302,6 +310,23 @@ PBT_UNROLL
         a_cols(1 + M);
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
+        if constexpr (kKeepLU<Num, M>) {
+            // The refined solve's first pass keeps the FP32 factors of R_q for
+            // its corrections (k_refine_step), as floats in aw, tiled by warp:
+            // for row q and this CTA's 32 systems, (M*M + 1) runs of 32 floats
+            // (factor (i, j) in run i + M*j, the pivot code in run M*M), so a
+            // warp writes 4*32*(M*M + 1) contiguous bytes a row, streaming
+            // (evict-first: they are read once, a whole sweep later).
+            if (g.aw != nullptr && active && ok) {
+                float* lf = reinterpret_cast<float*>(g.aw) +
+                            ((size_t)q * gridDim.x + blockIdx.x) * (size_t)(32 * (M * M + 1)) + lane;
+PBT_UNROLL
+                for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) __stcs(lf + 32 * (i + M * j), lu.f[i][j]);
+                __stcs(lf + 32 * M * M, __uint_as_float(lu.piv));
+            }
+        }
         lu_solve<Num, M>(lu, xd, y);
         if constexpr (staged_rolled<Num, M>()) {
 PBT_UNROLL
@@ -329,10 +354,14 @@ PBT_UNROLL
 PBT_UNROLL
                 for (int i = 0; i < M; ++i, pw += plane) {
                     if (active && ok) {
-                        if (raw || !Num::kConv)
+                        if constexpr (kFloatCW) {
+                            reinterpret_cast<float*>(g.cw)[(size_t)(s0 + lane) + o + plane0 * (size_t)(i + M * j)] =
+                                xj[i];
+                        } else if (raw || !Num::kConv) {
                             Num::sts(pw, xj[i]);
-                        else
+                        } else {
                             Num::out(pw, xj[i]);
+                        }
                     }
                     Num::sts(cps + 32 * (i * M + j), xj[i]);
                 }
@@ -366,8 +395,14 @@ PBT_UNROLL
 PBT_UNROLL
             for (int k = 0; k < M; ++k) {
                 const double* p = take();
+                if constexpr (kFloatCW) {
+                    const float* pf = reinterpret_cast<const float*>(p - lane) + lane;
 PBT_UNROLL
-                for (int i = 0; i < M; ++i) c[i][k] = fac_in<Num>(p + 32 * i, raw);
+                    for (int i = 0; i < M; ++i) c[i][k] = pf[32 * i];
+                } else {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) c[i][k] = fac_in<Num>(p + 32 * i, raw);
+                }
                 const CUtensorMap* nm = bwd_next(b, k, nrow_, nz);
                 give(nm, nrow_, nz);
             }

@@ -229,6 +229,29 @@ def test_refined_row_scaled(cuda, delta, nseg):
     assert err <= REFINE_TOL
 
 
+@pytest.mark.parametrize("m,nsys,nrow", [(1, 64, 30), (2, 100, 50), (4, 96, 20), (5, 256, 128), (6, 64, 40)])
+@pytest.mark.parametrize("delta", [1.05, 2.0])
+def test_refine_fused_correction_matches_separate_passes(cuda, m, nsys, nrow, delta):
+    """A single-segment refined plan whose first FP32 pass runs the staged
+    kernel keeps that pass's factors and runs each correction as one fused
+    pass (FP64 residual, FP32 substitution, accumulate); forcing direct loads
+    leaves no factors, so the corrections run as residual, FP32 solve and
+    accumulate.  They are the same operations: the same bits."""
+    w = synth.dominant(m, nsys, nrow, seed=900 + m, delta=delta)
+    outs = []
+    for kw in ({}, {"direct_loads": True}):
+        a, b, c, d = to_dev(w.arrays, cuda)
+        with pbt.BtdmaGpuPlan() as plan:
+            plan.create(m, nsys, nrow, 1, precision="fp32_refine", tol=1e-13, **kw)
+            pbt.solve_noncyclic(plan, a, b, c, d, m, nsys, nrow)
+            outs.append((d.cpu(), plan.refine_info()))
+    assert outs[0][1][0] >= 2
+    assert outs[0][1] == outs[1][1]
+    assert torch.equal(outs[0][0], outs[1][0])
+    ref = oracle_solve(w)
+    assert per_system_relerr(m, nsys, nrow, outs[0][0].numpy(), ref.D) <= REFINE_TOL
+
+
 def test_refine_stops_at_max_iter(cuda):
     w = synth.dominant(3, 64, 40, seed=5, delta=1.05)
     a, b, c, d = to_dev(w.arrays, cuda)
