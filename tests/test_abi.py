@@ -218,3 +218,39 @@ def test_heat3d_blocks_match_reference_stencil():
     row0 = [el(a, q, 0, 0), el(a, q, 0, 1), el(b, q, 0, 0), el(b, q, 0, 1), el(c, q, 0, 0), el(c, q, 0, 1)]
     assert np.allclose(row0, [sigma, -16 * sigma, 1 + 30 * sigma, -16 * sigma, sigma, 0.0])
     assert el(a, 0, 0, 0) == 0.0 and el(c, nblk - 1, 1, 1) == 0.0
+
+
+def test_lines_helpers_and_host_checks():
+    """pbt_lines from the host helpers, and the lines solve's checks that run
+    before any device call."""
+    import numpy as np
+
+    from pascal_btdma_gb300 import shared
+
+    L = pbt.Lines.packed(300, 64)
+    assert (L.nsys_inner, L.nsys_outer, L.stride_inner, L.stride_outer, L.row_stride, L.elem_stride) == \
+        (300, 1, 1, 0, 300, 300 * 64)
+    # Lines of a C-ordered (6, 5, 4) array along each axis, blocks of 2 points.
+    shape = (6, 5, 4)
+    a = np.arange(np.prod(shape)).reshape(shape)
+    for axis in range(3):
+        if shape[axis] % 2:
+            with pytest.raises(ValueError):
+                shared.Lines.axis(shape, axis, 2)
+            continue
+        L = shared.Lines.axis(shape, axis, 2)
+        flat = a.reshape(-1)
+        others = [x for x in range(3) if x != axis]
+        for s_out in range(L.nsys_outer):
+            for s_in in range(L.nsys_inner):
+                for q in range(shape[axis] // 2):
+                    for i in range(2):
+                        idx = [0, 0, 0]
+                        idx[others[0]], idx[others[1]], idx[axis] = s_out, s_in, 2 * q + i
+                        off = s_in * L.stride_inner + s_out * L.stride_outer + q * L.row_stride + i * L.elem_stride
+                        assert flat[off] == a[tuple(idx)]
+    # The C struct mirrors the header's field order.
+    c = L.c()
+    assert isinstance(c, N.Lines) and c.row_stride == L.row_stride
+    with pytest.raises(RuntimeError):
+        pbt.solve_noncyclic_lines(pbt.BtdmaGpuPlan(), None, None, None, None, L)
