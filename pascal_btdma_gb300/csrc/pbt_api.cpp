@@ -183,6 +183,17 @@ cudaError_t run_accumulate(int m, const pbt::SolveArgs& g, double* X, const doub
 cudaError_t run_refine_step(int m, const pbt::SolveArgs& g, const pbt::RefineArgs& ra) {
     PBT_DISPATCH_PLAIN_M(launch_refine_step, g, ra)
 }
+cudaError_t run_refine_staged(int m, const pbt::SolveArgs& g, const pbt::ThomasMaps& maps, const pbt::RefineArgs& ra) {
+    switch (m) {
+        case 1: return pbt::launch_refine_staged<1>(g, maps, ra);
+        case 2: return pbt::launch_refine_staged<2>(g, maps, ra);
+        case 3: return pbt::launch_refine_staged<3>(g, maps, ra);
+        case 4: return pbt::launch_refine_staged<4>(g, maps, ra);
+        case 5: return pbt::launch_refine_staged<5>(g, maps, ra);
+        case 6: return pbt::launch_refine_staged<6>(g, maps, ra);
+        default: return cudaErrorInvalidValue;
+    }
+}
 
 PBT_DISPATCH(run_thomas, launch_thomas)
 
@@ -521,8 +532,18 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
         if (fused) {
             const pbt::RefineArgs ra{reinterpret_cast<const float*>(p->aw), reinterpret_cast<float*>(p->re_), d,
                                      p->rstat};
-            if ((e = run_refine_step(m, g64, ra)) != cudaSuccess)
-                return cuda_fail(e, "refined solve: correction launch");
+            // The forward sweep's FP64 inputs through the TMA ring when the
+            // maps encode (k_refine_staged), else plain loads (k_refine_step).
+            const int mm = m * m;
+            pbt::ThomasMaps maps{};
+            if (encode_columns(&maps.a, a, ds.nsys, ds.nrow, mm, m) &&
+                encode_columns(&maps.b, b, ds.nsys, ds.nrow, mm, m) &&
+                encode_columns(&maps.c, c, ds.nsys, ds.nrow, mm, m) &&
+                encode_columns(&maps.d, rhs, ds.nsys, ds.nrow, m, m))
+                e = run_refine_staged(m, g64, maps, ra);
+            else
+                e = run_refine_step(m, g64, ra);
+            if (e != cudaSuccess) return cuda_fail(e, "refined solve: correction launch");
         } else {
             if ((e = run_residual(m, g64, d, p->re_)) != cudaSuccess)
                 return cuda_fail(e, "refined solve: residual launch");

@@ -32,5 +32,8 @@ template cudaError_t launch_gradients<PBT_M>(const SolveArgs&, const AdjointArgs
 template cudaError_t launch_residual<PBT_M>(const SolveArgs&, const double*, double*);
 template cudaError_t launch_accumulate<PBT_M>(const SolveArgs&, double*, const double*, unsigned*);
 template cudaError_t launch_refine_step<PBT_M>(const SolveArgs&, const RefineArgs&);
+#if PBT_M <= 6
+template cudaError_t launch_refine_staged<PBT_M>(const SolveArgs&, const ThomasMaps&, const RefineArgs&);
+#endif
 #endif
 }  // namespace pbt

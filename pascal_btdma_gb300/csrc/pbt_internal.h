@@ -98,6 +98,7 @@ struct RefineArgs {
     unsigned* stat;
 };
 template <int M> cudaError_t launch_refine_step(const SolveArgs& g, const RefineArgs& ra);
+template <int M> cudaError_t launch_refine_staged(const SolveArgs& g, const ThomasMaps& maps, const RefineArgs& ra);
 
 // Layout conversion for PBT_FLAG_CPU_LAYOUT plans (pbt_layout.cu): E elements
 // per (system, row); dir 0: CPU layout src -> GPU layout dst, 1: back.

@@ -449,6 +449,242 @@ PBT_UNROLL
     if (bad && active) atomicAdd(g.status, 1ull);
 }
 
+// ---------------------------------------------------------------------------
+// k_refine_staged: one correction of the refined solve (the work of
+// k_refine_step, the same operations in the same order, so the same bits)
+// with the forward sweep's FP64 inputs -- d (here the kept right-hand side),
+// the B, A and C columns, 1 + 3m items a row in that order -- staged through
+// a TMA ring as in k_thomas_staged.  Nothing else lives in shared memory, so
+// the ring is longer.  The factors, x and the backward sweep's C' and y use
+// plain loads (a fifth of the traffic).
+template <int M>
+__host__ __device__ constexpr int refine_ring() {
+    return kStagedSmemBudget / (M * 256 + 8) > 3 * (1 + 3 * M) ? 3 * (1 + 3 * M) : kStagedSmemBudget / (M * 256 + 8);
+}
+
+template <int M>
+__global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS)
+    k_refine_staged(const __grid_constant__ ThomasMaps maps, const SolveArgs g, const RefineArgs ra) {
+    constexpr int R = refine_ring<M>();
+    constexpr int K = 1 + 3 * M;  // items a row
+    constexpr unsigned kSlotBytes = M * 32 * 8;
+    extern __shared__ __align__(128) double ring[];
+    __shared__ __align__(8) unsigned long long bars[R];
+
+    const int lane = threadIdx.x;
+    const int s0 = blockIdx.x * 32;
+    const int sys = s0 + lane;
+    const bool active = sys < g.nsys;
+    const int N = g.nrow;
+    const size_t plane0 = (size_t)g.nsys * N;
+    const size_t rs = (size_t)g.nsys;
+    const size_t ngroups = ((size_t)g.nsys + 31) / 32;
+    const unsigned ring_s = smem_u32(ring), bar_s = smem_u32(bars);
+    const float* const C32 = reinterpret_cast<const float*>(g.cw);
+
+    if (lane == 0) {
+        for (int j = 0; j < R; ++j) mbar_init(bar_s + 8u * j, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+
+    int slot = 0;
+    unsigned phase = 0;
+    int n_cons = 0;
+    bool ok = true;
+    const int n_end = N * K;
+    auto issue = [&](int s, const CUtensorMap* map, int row, int z) {
+        mbar_expect_tx(bar_s + 8u * s, kSlotBytes);
+        tma_load_3d(ring_s + kSlotBytes * s, map, s0, row, z, bar_s + 8u * s);
+    };
+    auto take = [&]() -> const double* {
+        if (ok) ok = __all_sync(0xffffffffu, mbar_wait(bar_s + 8u * slot, phase));
+        return ring + slot * (M * 32) + lane;
+    };
+    // Release the current item (item n_cons) and refill its slot with item
+    // n_cons + R, if the sweep has one.
+    auto give = [&]() {
+        if (!ok) return;
+        __syncwarp();
+        const int nn = n_cons + R;
+        if (lane == 0 && nn < n_end) {
+            int z;
+            const CUtensorMap* mp = fwd_item<F64, M>(maps, nn % K, z);
+            fence_proxy_async_shared();
+            issue(slot, mp, nn / K, z);
+        }
+        ++n_cons;
+        if (++slot == R) {
+            slot = 0;
+            phase ^= 1u;
+        }
+    };
+    if (lane == 0) {
+        for (int j = 0; j < R && j < n_end; ++j) {
+            int z;
+            const CUtensorMap* mp = fwd_item<F64, M>(maps, j % K, z);
+            issue(j, mp, j / K, z);
+        }
+    }
+
+    double xm[M], x0[M], xp[M];
+    float y[M];
+PBT_UNROLL
+    for (int k = 0; k < M; ++k) {
+        xm[k] = 0.0;
+        x0[k] = active ? ra.x[sys + (size_t)k * plane0] : 0.0;
+        y[k] = 0.f;
+    }
+    for (int q = 0; q < N; ++q) {
+        const size_t o = (size_t)q * rs + sys;
+        const size_t plane = opaque(plane0);
+        const bool has_next = (q + 1 < N);
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) xp[k] = (has_next && active) ? ra.x[o + rs + (size_t)k * plane] : 0.0;
+        double r[M];
+        float an[M][M];
+        {
+            const double* p = take();
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) r[i] = p[32 * i];
+            give();
+        }
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) {
+            const double* p = take();
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) r[i] = fma(-p[32 * i], x0[k], r[i]);
+            give();
+        }
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) {
+            const double* p = take();
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                const double a = p[32 * i];
+                if (q > 0) r[i] = fma(-a, xm[k], r[i]);
+                an[i][k] = FF::split(a).h;
+            }
+            give();
+        }
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) {
+            const double* p = take();
+            if (has_next) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) r[i] = fma(-p[32 * i], xp[k], r[i]);
+            }
+            give();
+        }
+        if (!ok) break;
+        F32::Acc ta[M];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) ta[i] = F32::acc(FF::split(r[i]).h);
+        if (q > 0) {
+PBT_UNROLL
+            for (int k = 0; k < M; ++k)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) F32::msub(ta[i], an[i][k], y[k]);
+        }
+        LU<F32, M> lu;
+        if (active) {
+            const float* lf = ra.lu + ((size_t)q * ngroups + blockIdx.x) * (size_t)(32 * (M * M + 1)) + lane;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) lu.f[i][j] = __ldcs(lf + 32 * (i + M * j));
+            lu.piv = __float_as_uint(__ldcs(lf + 32 * M * M));
+        } else {
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) lu.f[i][j] = (i == j) ? 1.f : 0.f;
+            lu.piv = 0;
+PBT_UNROLL
+            for (int k = 0; k + 1 < M; ++k) lu.piv |= (unsigned)k << (4 * k);
+        }
+        lu.swaps = 0;
+PBT_UNROLL
+        for (int k = 0; k + 1 < M; ++k)
+            if (__any_sync(0xffffffffu, ((lu.piv >> (4 * k)) & 15u) != (unsigned)k)) lu.swaps |= 1u << k;
+        lu_solve<F32, M>(lu, ta, y);
+        if (active) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) ra.y[o + (size_t)i * plane] = y[i];
+        }
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) {
+            xm[k] = x0[k];
+            x0[k] = xp[k];
+        }
+    }
+
+    if (!ok) {
+        // A wait ran out: report it, then wait (boundedly) for the copies
+        // still in flight so none lands in shared memory after the CTA ends.
+        if (lane == 0) {
+            atomicAdd(g.status, kStallMark);
+            int s = slot;
+            unsigned ph = phase;
+            for (int j = 0; j < R && n_cons + j < n_end; ++j) {
+                if (!mbar_try_wait(bar_s + 8u * s, ph)) mbar_wait_slow(bar_s + 8u * s, ph, kWaitLimitNs / 4);
+                if (++s == R) {
+                    s = 0;
+                    ph ^= 1u;
+                }
+            }
+        }
+        __syncwarp();
+        return;
+    }
+    if (!active) return;
+    double emax = 0.0, xmax = 0.0;
+    float e[M];
+    for (int q = N - 1; q >= 0; --q) {
+        const size_t o = (size_t)q * rs + sys;
+        const size_t plane = opaque(plane0);
+        F32::Acc v[M];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) v[i] = F32::acc(ra.y[o + (size_t)i * plane]);
+        if (q < N - 1) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) F32::msub(v[i], __ldg(C32 + o + (size_t)(i + M * k) * plane), e[k]);
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            e[i] = F32::fin(v[i]);
+            double* px = ra.x + o + (size_t)i * plane;
+            const double ed = FF::widen(e[i]);
+            const double x = *px + ed;
+            *px = x;
+            emax = fmax(emax, fabs(ed));
+            xmax = fmax(xmax, fabs(x));
+        }
+    }
+    // NaN-safe: a non-finite or undefined ratio reports +Inf.
+    float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
+    if (!(ratio == ratio)) ratio = INFINITY;
+    atomicMax(ra.stat, __float_as_uint(ratio));
+}
+
+template <int M>
+cudaError_t launch_refine_staged(const SolveArgs& g, const ThomasMaps& maps, const RefineArgs& ra) {
+    if (M > kStagedMaxBlock) return cudaErrorNotSupported;
+    constexpr int smem = refine_ring<M>() * M * 32 * 8;
+    static bool configured = false;  // per instantiation; idempotent, so a race is harmless
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_refine_staged<M>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    const unsigned grid = (unsigned)((g.nsys + 31) / 32);
+    k_refine_staged<M><<<grid, 32, smem, g.stream>>>(maps, g, ra);
+    return cudaGetLastError();
+}
+
 template <class Num, int M>
 cudaError_t launch_thomas_staged(const SolveArgs& g, const ThomasMaps& maps) {
     if (M > kStagedMaxBlock) return cudaErrorNotSupported;
