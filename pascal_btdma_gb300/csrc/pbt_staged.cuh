@@ -640,17 +640,45 @@ PBT_UNROLL
     if (!active) return;
     double emax = 0.0, xmax = 0.0;
     float e[M];
+    // Backward, on plain loads: row q's C' and y are loaded while row q+1
+    // finishes (the forward sweep's registers are free by now).
+    float cn[M][M], yn[M];
+PBT_UNROLL
+    for (int i = 0; i < M; ++i)
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) cn[i][k] = 0.f;
+    {
+        const size_t o = (size_t)(N - 1) * rs + sys;
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) yn[i] = ra.y[o + (size_t)i * plane0];
+    }
     for (int q = N - 1; q >= 0; --q) {
         const size_t o = (size_t)q * rs + sys;
         const size_t plane = opaque(plane0);
+        float cq[M][M], yq[M];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            yq[i] = yn[i];
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) cq[i][k] = cn[i][k];
+        }
+        if (q > 0) {
+            const size_t op = o - rs;
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                yn[i] = ra.y[op + (size_t)i * plane];
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) cn[i][k] = __ldg(C32 + op + (size_t)(i + M * k) * plane);
+            }
+        }
         F32::Acc v[M];
 PBT_UNROLL
-        for (int i = 0; i < M; ++i) v[i] = F32::acc(ra.y[o + (size_t)i * plane]);
+        for (int i = 0; i < M; ++i) v[i] = F32::acc(yq[i]);
         if (q < N - 1) {
 PBT_UNROLL
             for (int i = 0; i < M; ++i)
 PBT_UNROLL
-                for (int k = 0; k < M; ++k) F32::msub(v[i], __ldg(C32 + o + (size_t)(i + M * k) * plane), e[k]);
+                for (int k = 0; k < M; ++k) F32::msub(v[i], cq[i][k], e[k]);
         }
 PBT_UNROLL
         for (int i = 0; i < M; ++i) {
