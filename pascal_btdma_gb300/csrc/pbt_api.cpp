@@ -294,7 +294,9 @@ bool prefer_staged(int arith, int m, int nsys, int sms) {
     return (m == 5 || m == 6) && small;
 }
 
-cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveArgs& g, bool* ran_staged = nullptr) {
+// Whether the single-segment solve of g runs with TMA-staged loads; if so,
+// the tensor maps are filled.
+bool thomas_stages(const pbt_plan* p, int arith, int m, const pbt::SolveArgs& g, pbt::ThomasMaps* maps) {
     const pbt_plan_desc& ds = p->desc;
     bool staged;
     if (ds.flags & PBT_FLAG_DIRECT_LOADS)
@@ -303,19 +305,17 @@ cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveA
         staged = true;
     else
         staged = prefer_staged(arith, m, g.nsys, p->sms);
-    if (staged && m <= pbt::kStagedMaxBlock && g.nsys >= 32) {
-        pbt::ThomasMaps maps;
-        const int mm = m * m;
-        if (encode_columns(&maps.a, g.a, g.nsys, g.nrow, mm, m) && encode_columns(&maps.b, g.b, g.nsys, g.nrow, mm, m) &&
-            encode_columns(&maps.c, g.c, g.nsys, g.nrow, mm, m) && encode_columns(&maps.d, g.d, g.nsys, g.nrow, m, m) &&
-            (arith == kF32 ? encode_columns_f32(&maps.w, g.cw, g.nsys, g.nrow, mm, m)
-                           : encode_columns(&maps.w, g.cw, g.nsys, g.nrow, mm, m))) {
-            if (ran_staged) *ran_staged = true;
-            return run_thomas_staged(arith, m, g, maps);
-        }
-    }
-    if (ran_staged) *ran_staged = false;
-    return run_thomas(arith, m, g);
+    if (!staged || m > pbt::kStagedMaxBlock || g.nsys < 32) return false;
+    const int mm = m * m;
+    return encode_columns(&maps->a, g.a, g.nsys, g.nrow, mm, m) && encode_columns(&maps->b, g.b, g.nsys, g.nrow, mm, m) &&
+           encode_columns(&maps->c, g.c, g.nsys, g.nrow, mm, m) && encode_columns(&maps->d, g.d, g.nsys, g.nrow, m, m) &&
+           (arith == kF32 ? encode_columns_f32(&maps->w, g.cw, g.nsys, g.nrow, mm, m)
+                          : encode_columns(&maps->w, g.cw, g.nsys, g.nrow, mm, m));
+}
+
+cudaError_t thomas_launch(const pbt_plan* p, int arith, int m, const pbt::SolveArgs& g) {
+    pbt::ThomasMaps maps;
+    return thomas_stages(p, arith, m, g, &maps) ? run_thomas_staged(arith, m, g, maps) : run_thomas(arith, m, g);
 }
 
 // Whether a two-stage plan solves its reduced system (nsys lines of `rn`
@@ -510,18 +510,23 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
         return e;
     };
     double* const rhs = p->rx;
-    cudaError_t e = cudaMemcpyAsync(rhs, d, nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return cuda_fail(e, "refined solve: set-up copy");
-    // A single-segment plan whose first pass ran the staged kernel has the
-    // FP32 factors (in p->aw); its corrections are then one k_refine_step
-    // each.  Otherwise: residual, FP32 solve, accumulate.
-    bool staged = false;
-    if (p->thomas)
-        e = thomas_launch(p, kF32, m, make_args(p, a, b, c, d, s, ds.nsys), &staged);
-    else
-        e = fp32_solve(d);
+    // A single-segment plan whose first pass runs the staged kernel keeps the
+    // FP32 factors (in p->aw) and copies d into rhs as it reads it; its
+    // corrections are then one fused pass each.  Otherwise: d copied first,
+    // and residual, FP32 solve, accumulate per correction.
+    pbt::SolveArgs g1 = make_args(p, a, b, c, d, s, ds.nsys);
+    pbt::ThomasMaps maps1;
+    const bool fused = p->thomas && p->aw != nullptr && m <= pbt::kStagedMaxBlock && thomas_stages(p, kF32, m, g1, &maps1);
+    cudaError_t e;
+    if (fused) {
+        g1.ra = rhs;
+        e = run_thomas_staged(kF32, m, g1, maps1);
+    } else {
+        e = cudaMemcpyAsync(rhs, d, nv * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return cuda_fail(e, "refined solve: set-up copy");
+        e = p->thomas ? thomas_launch(p, kF32, m, g1) : fp32_solve(d);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "refined solve: FP32 solve launch");
-    const bool fused = staged && p->aw != nullptr && m <= pbt::kStagedMaxBlock;
     p->last_iters = 1;
     p->last_correction = 1.0;
     const pbt::SolveArgs g64 = make_args(p, a, b, c, rhs, s, ds.nsys);

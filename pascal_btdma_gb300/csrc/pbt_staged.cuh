@@ -267,6 +267,14 @@ __global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const
             const double* p = take();
 PBT_UNROLL
             for (int i = 0; i < M; ++i) xd[i] = Num::acc(Num::in(p + 32 * i));
+            if constexpr (kKeepLU<Num, M>) {
+                // The refined solve's first pass keeps the right-hand side
+                // (in g.ra) as it streams by: D is solved in place.
+                if (g.ra != nullptr && active && ok) {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) g.ra[(size_t)(s0 + lane) + o + plane0 * (size_t)i] = p[32 * i];
+                }
+            }
             const CUtensorMap* nm = fwd_next(q, 0, nrow_, nz);
             give(nm, nrow_, nz);
         }
