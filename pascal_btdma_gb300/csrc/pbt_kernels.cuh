@@ -1484,10 +1484,13 @@ PBT_UNROLL
 // (the operations of the FP32 solve, so e is the FP32 solve of r bit for bit;
 // the factors come from ra.lu, tiled by warp as the staged pass wrote them);
 // backward: e_q = y_q - C'_q e_{q+1} with the FP32 pass's C' (floats, as the
-// staged FP32 kernel keeps them), and x_q += e_q
-// with the convergence statistic of k_accumulate.  It reads A, B, C once per
+// staged FP32 kernel keeps them), and x_q += e_q with the convergence
+// statistic of k_accumulate.  It reads A, B, C once per
 // correction where the separate residual, FP32 solve and accumulate read them
-// twice and move x and r three more times.
+// twice and move x and r three more times.  One thread per system, plain
+// loads: the refined solve uses k_refine_staged (the same operations with the
+// forward inputs staged through a TMA ring) and falls back to this kernel
+// when the tensor maps cannot be encoded.
 template <int M>
 __global__ void __launch_bounds__(64) k_refine_step(const SolveArgs g, const RefineArgs ra) {
     if constexpr (M > kStagedMaxBlock) {
