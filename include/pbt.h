@@ -191,7 +191,11 @@ typedef struct pbt_lines {
  * A PBT_FLAG_INPLACE plan writes C' into C, as the reference does; any other
  * plan keeps its factors in its workspace, addressed with the same strides,
  * so the lines must then fit in nsys*nrow*m*m elements (a dense layout, as
- * euler3d's), else PBT_EUNSUPPORTED.  Always the direct-load kernel. */
+ * euler3d's), else PBT_EUNSUPPORTED.  Lines whose rows are contiguous
+ * (row_stride 1, stride_inner != 1: a sweep along the array's fast index,
+ * which one thread per line would read uncoalesced) are transposed into plan
+ * workspace (the inputs' size, allocated on the first such call), solved in
+ * the reference layout and transposed back; no extent rule applies there. */
 int pbt_solve_noncyclic_lines(pbt_plan* plan, double* a, double* b, double* c, double* d,
                               const pbt_lines* lines, void* stream);
 

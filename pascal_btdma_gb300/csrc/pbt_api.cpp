@@ -851,19 +851,52 @@ int pbt_solve_noncyclic_lines(pbt_plan* p, double* a, double* b, double* c, doub
     }
     if (L->stride_inner < 0 || L->stride_outer < 0 || L->row_stride < 0 || L->elem_stride < 0)
         return fail(PBT_EINVAL, "solve_lines: negative stride");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const pbt::LineStrides ls{L->nsys_inner, L->stride_inner, L->stride_outer, L->row_stride, L->elem_stride};
+    const bool inplace = (ds.flags & PBT_FLAG_INPLACE) != 0;
+    if (L->row_stride == 1 && L->stride_inner != 1) {
+        // Rows contiguous, lines not (a sweep along the array's fast index):
+        // one thread per line would read 32 lines per warp load.  Tiled
+        // transposes into plan workspace (allocated on first use), the
+        // reference-layout solve, and the solution (and, in place, C') back.
+        const int m = ds.m, nsys = ds.nsys, nrow = ds.nrow;
+        const size_t rows = (size_t)nsys * nrow, mmz = (size_t)m * m;
+        if (!p->la) {
+            const size_t bytes0 = p->bytes;
+            if ((rc = alloc(p, &p->la, mmz * rows)) || (rc = alloc(p, &p->lb, mmz * rows)) ||
+                (rc = alloc(p, &p->lc, mmz * rows)) || (rc = alloc(p, &p->ld, (size_t)m * rows))) {
+                cudaFree(p->la);
+                cudaFree(p->lb);
+                cudaFree(p->lc);
+                cudaFree(p->ld);
+                p->la = p->lb = p->lc = p->ld = nullptr;
+                p->bytes = bytes0;
+                return rc;
+            }
+        }
+        p->last_stream = s;
+        cudaError_t e = pbt::launch_lines_layout(a, p->la, ls, m * m, nsys, nrow, 0, s);
+        if (e == cudaSuccess) e = pbt::launch_lines_layout(b, p->lb, ls, m * m, nsys, nrow, 0, s);
+        if (e == cudaSuccess) e = pbt::launch_lines_layout(c, p->lc, ls, m * m, nsys, nrow, 0, s);
+        if (e == cudaSuccess) e = pbt::launch_lines_layout(d, p->ld, ls, m, nsys, nrow, 0, s);
+        if (e != cudaSuccess) return cuda_fail(e, "solve_lines: transpose in");
+        rc = solve_core(p, p->la, p->lb, p->lc, p->ld, m, nsys, nrow, false, nullptr, s);
+        if (rc) return rc;
+        e = pbt::launch_lines_layout(p->ld, d, ls, m, nsys, nrow, 1, s);
+        if (e == cudaSuccess && inplace) e = pbt::launch_lines_layout(p->lc, c, ls, m * m, nsys, nrow, 1, s);
+        if (e != cudaSuccess) return cuda_fail(e, "solve_lines: transpose out");
+        return PBT_OK;
+    }
     const long long mm = (long long)ds.m * ds.m;
     // One past the last element a block array is addressed at.
     const long long extent = (long long)(L->nsys_inner - 1) * L->stride_inner +
                              (long long)(L->nsys_outer - 1) * L->stride_outer +
                              (long long)(ds.nrow - 1) * L->row_stride + (mm - 1) * L->elem_stride + 1;
-    const bool inplace = (ds.flags & PBT_FLAG_INPLACE) != 0;
     if (!inplace && extent > mm * ds.nsys * ds.nrow)
         return fail(PBT_EUNSUPPORTED,
                     "solve_lines: the lines span more than the plan's factor workspace (nsys*nrow*m*m); "
                     "use a PBT_FLAG_INPLACE plan for a non-dense layout");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     p->last_stream = s;
-    const pbt::LineStrides ls{L->nsys_inner, L->stride_inner, L->stride_outer, L->row_stride, L->elem_stride};
     cudaError_t e = run_thomas_lines(arith_of(ds.precision), ds.m, make_args(p, a, b, c, d, s, ds.nsys), ls);
     if (e != cudaSuccess) return cuda_fail(e, "block Thomas launch (strided lines)");
     return PBT_OK;

@@ -66,6 +66,10 @@ constexpr unsigned long long kStallMark = 1ull << 48;
 // (1..PBT_MAX_BLOCK) in pbt_inst.cu.  Each returns cudaGetLastError().
 template <class Num, int M> cudaError_t launch_thomas(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_thomas_lines(const SolveArgs& g, const LineStrides& ls);
+// Lines with row stride 1 <-> the reference GPU layout, E element planes
+// (dir 0: lines -> reference; dir 1: back).
+cudaError_t launch_lines_layout(const double* src, double* dst, const LineStrides& ls, int E, int nsys, int nrow,
+                                int dir, cudaStream_t s);
 template <class Num, int M> cudaError_t launch_thomas_staged(const SolveArgs& g, const ThomasMaps& maps);
 template <class Num, int M> cudaError_t launch_modi(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced(const SolveArgs& g);

@@ -73,7 +73,64 @@ __global__ void k_ff_raw_f64(double* x, size_t n, int to_f64) {
     }
 }
 
+// Lines whose rows are contiguous (row stride 1: a sweep along an array's
+// fast index) <-> the reference GPU layout.  One CTA moves a tile of 32 rows
+// x 32 systems of one element plane: the lines side is read (or written) along
+// the rows, the reference side along the systems, both in 256-byte runs, and
+// the tile turns around in shared memory (stride 33).  dir 0: lines (src) ->
+// reference (dst); dir 1: reference (src) -> lines (dst).
+__global__ void __launch_bounds__(256) k_lines_layout(const double* __restrict__ src, double* __restrict__ dst,
+                                                      LineStrides ls, int nsys, int nrow, int dir) {
+    __shared__ double tile[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8 threads, 4 tile rows each
+    const int r0 = blockIdx.x * 32, e = blockIdx.z;
+    const int nsb = (nsys + 31) / 32;
+    auto app = [&](int s, int r) {
+        return (size_t)(s % ls.lin) * (size_t)ls.in + (size_t)(s / ls.lin) * (size_t)ls.out + (size_t)r +
+               (size_t)e * (size_t)ls.elem;
+    };
+    auto ref = [&](int s, int r) { return (size_t)s + (size_t)nsys * ((size_t)r + (size_t)nrow * e); };
+    for (int sb = blockIdx.y; sb < nsb; sb += gridDim.y) {
+        const int s0 = sb * 32;
+        if (dir == 0) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 8) {
+                const int r = r0 + tx, sy = s0 + ty + j;
+                if (r < nrow && sy < nsys) tile[ty + j][tx] = src[app(sy, r)];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 32; j += 8) {
+                const int sx = s0 + tx, r = r0 + ty + j;
+                if (r < nrow && sx < nsys) dst[ref(sx, r)] = tile[tx][ty + j];
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; j += 8) {
+                const int sx = s0 + tx, r = r0 + ty + j;
+                if (r < nrow && sx < nsys) tile[tx][ty + j] = src[ref(sx, r)];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 32; j += 8) {
+                const int r = r0 + tx, sy = s0 + ty + j;
+                if (r < nrow && sy < nsys) dst[app(sy, r)] = tile[ty + j][tx];
+            }
+        }
+        __syncthreads();  // the tile is reused by the next system block
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_lines_layout(const double* src, double* dst, const LineStrides& ls, int E, int nsys, int nrow,
+                                int dir, cudaStream_t s) {
+    if (E <= 0 || nsys <= 0 || nrow <= 0) return cudaSuccess;
+    const int nsb = (nsys + 31) / 32;
+    const dim3 grid((unsigned)((nrow + 31) / 32), (unsigned)(nsb < 65535 ? nsb : 65535), (unsigned)E);
+    k_lines_layout<<<grid, dim3(32, 8), 0, s>>>(src, dst, ls, nsys, nrow, dir);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_ff_raw_f64(double* x, size_t n, int to_f64, cudaStream_t s) {
     if (n == 0) return cudaSuccess;

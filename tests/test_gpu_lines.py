@@ -142,3 +142,29 @@ def test_lines_solve_refuses_other_plans(cuda):
             plan.create(m, nsys, nrow, nseg, **kw)
             with pytest.raises(NotImplementedError):
                 pbt.solve_noncyclic_lines(plan, *arrs, good)
+
+
+@pytest.mark.parametrize("m,prec,inplace", [(5, "ff", False), (3, "fp64", True), (2, "ff", True), (6, "fp64", False)])
+def test_fast_axis_lines_are_the_plain_solve(cuda, m, prec, inplace):
+    """Lines along the contiguous index (the x sweep: row stride 1) go through
+    tiled transposes into the reference layout and back: the plain solve's
+    bits, and in place C' back in the application's layout."""
+    sweep = "x"
+    (ra, ia, oa), _ = SWEEPS[sweep]
+    nrow, nsys = SHAPE[ra], SHAPE[ia] * SHAPE[oa]
+    w = synth.dominant(m, nsys, nrow, seed=90 + m)
+    app = [to_app(x, m * m if k < 3 else m, sweep, SHAPE) for k, x in enumerate(w.arrays)]
+    a, b, c, d = (torch.from_numpy(x).to(cuda) for x in app)
+    packed = [torch.from_numpy(x.copy()).to(cuda) for x in w.arrays]
+    with pbt.BtdmaGpuPlan() as plan:
+        plan.create(m, nsys, nrow, 1, precision=prec, inplace=inplace)
+        pbt.solve_noncyclic_lines(plan, a, b, c, d, sweep_lines(sweep, SHAPE, dense_strides(SHAPE)))
+    with pbt.BtdmaGpuPlan() as plan:
+        plan.create(m, nsys, nrow, 1, precision=prec, inplace=inplace, direct_loads=True)
+        pbt.solve_noncyclic(plan, *packed, m, nsys, nrow)
+    torch.cuda.synchronize()
+    assert np.array_equal(to_ref(d.cpu().numpy(), sweep), packed[3].cpu().numpy())
+    if inplace:
+        assert np.array_equal(to_ref(c.cpu().numpy(), sweep), packed[2].cpu().numpy())
+    else:
+        assert np.array_equal(c.cpu().numpy(), app[2])
