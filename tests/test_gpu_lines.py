@@ -144,21 +144,22 @@ def test_lines_solve_refuses_other_plans(cuda):
                 pbt.solve_noncyclic_lines(plan, *arrs, good)
 
 
+@pytest.mark.parametrize("shape", [SHAPE, (40, 7, 5)])  # (40, 7, 5): 35 lines of 40 rows, ragged 32-tiles
 @pytest.mark.parametrize("m,prec,inplace", [(5, "ff", False), (3, "fp64", True), (2, "ff", True), (6, "fp64", False)])
-def test_fast_axis_lines_are_the_plain_solve(cuda, m, prec, inplace):
+def test_fast_axis_lines_are_the_plain_solve(cuda, m, prec, inplace, shape):
     """Lines along the contiguous index (the x sweep: row stride 1) go through
     tiled transposes into the reference layout and back: the plain solve's
     bits, and in place C' back in the application's layout."""
     sweep = "x"
     (ra, ia, oa), _ = SWEEPS[sweep]
-    nrow, nsys = SHAPE[ra], SHAPE[ia] * SHAPE[oa]
+    nrow, nsys = shape[ra], shape[ia] * shape[oa]
     w = synth.dominant(m, nsys, nrow, seed=90 + m)
-    app = [to_app(x, m * m if k < 3 else m, sweep, SHAPE) for k, x in enumerate(w.arrays)]
+    app = [to_app(x, m * m if k < 3 else m, sweep, shape) for k, x in enumerate(w.arrays)]
     a, b, c, d = (torch.from_numpy(x).to(cuda) for x in app)
     packed = [torch.from_numpy(x.copy()).to(cuda) for x in w.arrays]
     with pbt.BtdmaGpuPlan() as plan:
         plan.create(m, nsys, nrow, 1, precision=prec, inplace=inplace)
-        pbt.solve_noncyclic_lines(plan, a, b, c, d, sweep_lines(sweep, SHAPE, dense_strides(SHAPE)))
+        pbt.solve_noncyclic_lines(plan, a, b, c, d, sweep_lines(sweep, shape, dense_strides(shape)))
     with pbt.BtdmaGpuPlan() as plan:
         plan.create(m, nsys, nrow, 1, precision=prec, inplace=inplace, direct_loads=True)
         pbt.solve_noncyclic(plan, *packed, m, nsys, nrow)
