@@ -254,3 +254,27 @@ def test_lines_helpers_and_host_checks():
     assert isinstance(c, N.Lines) and c.row_stride == L.row_stride
     with pytest.raises(RuntimeError):
         pbt.solve_noncyclic_lines(pbt.BtdmaGpuPlan(), None, None, None, None, L)
+
+
+def test_strided_runner_lines_address_the_euler3d_layout():
+    """The sweep runner's lines (python -m pascal_btdma_gb300.strided) address
+    element e of point (i, j, k) of a C-ordered [e, k, j, i] array: rows along
+    the sweep axis, lines over the other two."""
+    import numpy as np
+
+    from pascal_btdma_gb300 import strided
+
+    n, E = 4, 3
+    arr = np.arange(E * n ** 3).reshape(E, n, n, n)
+    flat = arr.reshape(-1)
+    for axis in "xyz":
+        L = strided.lines_of(n, axis)
+        for s_out in range(n):
+            for s_in in range(n):
+                for q in range(n):
+                    for e in range(E):
+                        off = s_in * L.stride_inner + s_out * L.stride_outer + q * L.row_stride + e * L.elem_stride
+                        i, j, k = {"x": (q, s_in, s_out), "y": (s_in, q, s_out), "z": (s_in, s_out, q)}[axis]
+                        assert flat[off] == arr[e, k, j, i]
+    with pytest.raises(ValueError):
+        strided.lines_of(n, "w")
