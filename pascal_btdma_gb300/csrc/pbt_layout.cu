@@ -22,6 +22,7 @@ namespace {
 
 constexpr int kTile = 32;
 constexpr int kThreads = 256;
+constexpr int kBatch = 4;  // loads a thread has in flight in k_layout
 
 // dir 0: CPU layout (src) -> GPU layout (dst); dir 1: GPU -> CPU.
 __global__ void __launch_bounds__(kThreads) k_layout(const double* __restrict__ src, double* __restrict__ dst,
@@ -34,10 +35,23 @@ __global__ void __launch_bounds__(kThreads) k_layout(const double* __restrict__ 
     const size_t cpu0 = (size_t)E * ((size_t)s0 + (size_t)nsys * row);  // first element of the tile, CPU layout
     const size_t gpu0 = (size_t)s0 + (size_t)nsys * row;                // (sys s0, row, e = 0), GPU layout
     const int total = cnt * E;
+    // Loads go out kBatch at a time before any of them is waited on.
     if (dir == 0) {
-        for (int t = threadIdx.x; t < total; t += kThreads) {
-            const int s = t / E, e = t - s * E;
-            tile[e * (kTile + 1) + s] = src[cpu0 + t];
+        for (int t0 = threadIdx.x; t0 < total; t0 += kBatch * kThreads) {
+            double v[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int t = t0 + u * kThreads;
+                v[u] = t < total ? src[cpu0 + t] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int t = t0 + u * kThreads;
+                if (t < total) {
+                    const int s = t / E, e = t - s * E;
+                    tile[e * (kTile + 1) + s] = v[u];
+                }
+            }
         }
         __syncthreads();
         for (int t = threadIdx.x; t < E * kTile; t += kThreads) {
@@ -45,9 +59,20 @@ __global__ void __launch_bounds__(kThreads) k_layout(const double* __restrict__ 
             if (s < cnt) dst[gpu0 + s + plane * e] = tile[e * (kTile + 1) + s];
         }
     } else {
-        for (int t = threadIdx.x; t < E * kTile; t += kThreads) {
-            const int e = t / kTile, s = t - e * kTile;
-            if (s < cnt) tile[e * (kTile + 1) + s] = src[gpu0 + s + plane * e];
+        for (int t0 = threadIdx.x; t0 < E * kTile; t0 += kBatch * kThreads) {
+            double v[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int t = t0 + u * kThreads;
+                const int e = t / kTile, s = t - e * kTile;
+                v[u] = (t < E * kTile && s < cnt) ? src[gpu0 + s + plane * e] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int t = t0 + u * kThreads;
+                const int e = t / kTile, s = t - e * kTile;
+                if (t < E * kTile && s < cnt) tile[e * (kTile + 1) + s] = v[u];
+            }
         }
         __syncthreads();
         for (int t = threadIdx.x; t < total; t += kThreads) {
