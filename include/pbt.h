@@ -75,10 +75,29 @@ typedef enum pbt_status {
     PBT_EUNSUPPORTED = 4, /* combination not provided (std::logic_error) */
     PBT_ENOMEM = 5,       /* device workspace allocation failed */
     PBT_ESINGULAR = 6,    /* a zero pivot was met in some block (pbt_plan_status) */
-    PBT_ETIMEOUT = 7      /* a bounded device-side wait ran out (pbt_plan_status); results invalid */
+    PBT_ETIMEOUT = 7,     /* a bounded device-side wait ran out (pbt_plan_status); results invalid */
+    PBT_ERANGE = 8,       /* a float-float / FP32 value left the arithmetic's range (pbt_plan_status);
+                             results invalid: solve with PBT_PREC_FP64 */
+    PBT_ENOCONV = 9       /* the refined solve did not reach desc.tol in desc.max_iter FP32 solves
+                             (pbt_plan_status) */
 } pbt_status;
 
-/* Arithmetic of the solve. */
+/* Arithmetic of the solve.
+ *
+ * Range of the float-float method.  Its values are pairs of FP32 numbers, so
+ * it has FP32's exponent range, not FP64's.  It accepts input entries (A, B,
+ * C, D, and the adjoint's dL/dx) that are zero or of magnitude
+ * 2^-96 <= |v| < 2^96 (about 1.3e-29 to 7.9e28).  Any other entry (a nonzero
+ * entry below 2^-96, one at or above 2^96, Inf, NaN), any overflow on the way,
+ * and any system whose solution lies wholly below 2^-100 in magnitude (where
+ * the pairs lose their 47 bits) turn the solve into a reported failure:
+ * pbt_plan_status returns PBT_ERANGE and the solution must not be used.  The
+ * outcome is never a silently wrong number.  Solve such systems with
+ * PBT_PREC_FP64, which has the reference's own range.
+ * The FP32-refined method reads entries below 2^-126 as zero and fails on
+ * entries at or above 2^128; its FP64 residual corrects the rest.  A
+ * refinement that cannot converge is reported: PBT_ERANGE if a correction came
+ * out Inf/NaN, else PBT_ENOCONV. */
 typedef enum pbt_precision {
     PBT_PREC_FP64 = 0,        /* plain FP64 arithmetic, partial-pivot LU per block */
     PBT_PREC_FF = 1,          /* FP64 data, float-float (two-FP32) arithmetic on the FP32 pipes */
@@ -99,7 +118,7 @@ typedef struct pbt_plan_desc {
     int m;                 /* block size, 1..PBT_MAX_BLOCK */
     int nsys;              /* number of independent systems */
     int nrow;              /* block rows per system (full line length N) */
-    int nseg;              /* segments per line (P); >= 3 rows each when P > 1 */
+    int nseg;              /* segments per line (P), 1..65535; >= 3 rows each when P > 1 */
     int precision;         /* pbt_precision */
     unsigned flags;        /* PBT_FLAG_* */
     double tol;            /* PBT_PREC_FP32_REFINE: target relative correction size */
@@ -195,7 +214,10 @@ typedef struct pbt_lines {
  * (row_stride 1, stride_inner != 1: a sweep along the array's fast index,
  * which one thread per line would read uncoalesced) are transposed into plan
  * workspace (the inputs' size, allocated on the first such call), solved in
- * the reference layout and transposed back; no extent rule applies there. */
+ * the reference layout and transposed back; no extent rule applies there.
+ * That first call allocates (cudaMalloc, which may synchronise the device and
+ * is not allowed during stream capture): make one such call before capturing
+ * a graph of these solves. */
 int pbt_solve_noncyclic_lines(pbt_plan* plan, double* a, double* b, double* c, double* d,
                               const pbt_lines* lines, void* stream);
 
@@ -216,9 +238,11 @@ int pbt_solve_noncyclic_lines(pbt_plan* plan, double* a, double* b, double* c, d
  * Limit: nsys * 2 * nseg * (2*m*m + m) doubles, each of the three reduced
  * arrays rounded up to a multiple of 32, must fit in 4 Mi doubles; larger
  * calls return PBT_EINVAL with the sizes in pbt_last_error_string().  Other
- * argument rules as pbt_plan_create.  The first call on each device looks up
- * the array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the array
+ * argument rules as pbt_plan_create (1 <= nseg <= 65535).  Every call looks
+ * up the array's device address (cudaGetSymbolAddress) on the current device,
+ * so a device reset between calls is harmless; the first call on a device
+ * also loads the library's device code there, so make that first call before
+ * any stream capture.  All calls share the array
  * and it keeps the previous call's contents (each call rewrites what it
  * reads), so two calls that overlap on the GPU race: serialise them on one
  * stream.  Zero pivots are not reported by this entry. */
@@ -232,9 +256,9 @@ int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, double* d,
  *   dL/dA_q = -lambda_q x_{q-1}^T,  dL/dB_q = -lambda_q x_q^T,  dL/dC_q = -lambda_q x_{q+1}^T,
  * with dL/dA_0 = dL/dC_{nrow-1} = 0.  x is the forward solution and a, b, c
  * the forward blocks, unchanged (the plan must not be PBT_FLAG_INPLACE).
- * nseg = 1, m <= 6: one fused kernel solves M^T lambda = g by block Thomas
+ * nseg = 1 (every m): one fused kernel solves M^T lambda = g by block Thomas
  * on the transposed blocks, read in place, and forms the gradient blocks in
- * its backward sweep.  Otherwise M^T's blocks are materialised in plan
+ * its backward sweep.  nseg > 1: M^T's blocks are materialised in plan
  * workspace (allocated by the first such call), solved by the plan's forward
  * method, and the gradients formed in one more pass.  Precision fp64 or ff. */
 int pbt_adjoint_noncyclic(pbt_plan* plan, const double* a, const double* b, const double* c,
@@ -243,10 +267,13 @@ int pbt_adjoint_noncyclic(pbt_plan* plan, const double* a, const double* b, cons
 
 /* Synchronises the plan's last stream and reports through *nsingular how
  * many zero pivots the solves since the previous call met (the reference has
- * no such report; its dgesv-less GPU path divides by zero silently).  Returns
- * PBT_ETIMEOUT if a kernel's bounded wait for its staged input ran out (the
- * solution of that solve is not valid), else PBT_ESINGULAR when
- * *nsingular > 0.  nsingular may be NULL. */
+ * no such report; its dgesv-less GPU path divides by zero silently).  Returns,
+ * in this order of precedence: PBT_ETIMEOUT if a kernel's bounded wait for its
+ * staged input ran out; PBT_ERANGE if a float-float or FP32 solve left its
+ * arithmetic's range (see pbt_precision); PBT_ESINGULAR when *nsingular > 0;
+ * PBT_ENOCONV if a refined solve did not reach its tolerance.  After
+ * PBT_ETIMEOUT and PBT_ERANGE the solution of that solve is not valid.  The
+ * call clears what it reports.  nsingular may be NULL. */
 int pbt_plan_status(pbt_plan* plan, long long* nsingular);
 
 /* Outcome of the last solve on a PBT_PREC_FP32_REFINE plan: the number of

@@ -17,7 +17,9 @@
  * std::invalid_argument, PBT_ECUDA -> CudaError, PBT_ESTATE and
  * PBT_ETIMEOUT -> std::runtime_error, PBT_EUNSUPPORTED -> std::logic_error,
  * PBT_ENOMEM -> std::bad_alloc, PBT_ESINGULAR -> pbt::SingularBlock (a
- * std::runtime_error; the reference has no such report).  Header only; link
+ * std::runtime_error; the reference has no such report), PBT_ERANGE ->
+ * pbt::ArithmeticRange (a std::range_error: a float-float / FP32 solve left its
+ * arithmetic's range), PBT_ENOCONV -> std::runtime_error.  Header only; link
  * libpbt.so.
  */
 #ifndef PBT_HPP
@@ -42,6 +44,11 @@ public:
     using std::runtime_error::runtime_error;
 };
 
+class ArithmeticRange : public std::range_error {
+public:
+    using std::range_error::range_error;
+};
+
 inline void check(int status, const char* where) {
     if (status == PBT_OK) return;
     const std::string msg = std::string(where) + ": " + pbt_last_error_string();
@@ -51,7 +58,8 @@ inline void check(int status, const char* where) {
         case PBT_EUNSUPPORTED: throw std::logic_error(msg);
         case PBT_ENOMEM: throw std::bad_alloc();
         case PBT_ESINGULAR: throw SingularBlock(msg);
-        default: throw std::runtime_error(msg);  // PBT_ESTATE, PBT_ETIMEOUT
+        case PBT_ERANGE: throw ArithmeticRange(msg);
+        default: throw std::runtime_error(msg);  // PBT_ESTATE, PBT_ETIMEOUT, PBT_ENOCONV
     }
 }
 

@@ -71,7 +71,9 @@ int pbt_batch_solve(pbt_batch* batch, const double* pa, const double* pb, const 
 
 /* Synchronises the last stream; reports zero pivots met and whether a wait
  * of the persistent kernel ran out (*timed_out = 1, the result is invalid).
- * Returns PBT_ESINGULAR / PBT_ECUDA accordingly. */
+ * Returns PBT_ECUDA (a wait ran out), PBT_ERANGE (a float-float batch left
+ * the arithmetic's range, as pbt_plan_status; the result is invalid) or
+ * PBT_ESINGULAR accordingly, in that order. */
 int pbt_batch_status(pbt_batch* batch, long long* nsingular, int* timed_out);
 
 /* Shape of the schedule: tiles, stage-1 and stage-3 items, persistent CTAs of

@@ -46,9 +46,10 @@ typedef struct pbt_shared pbt_shared;
  * factorisation runs on the host in FP64; the factors go to device memory on
  * the current device.  precision: PBT_PREC_FP64 (the solve in FP64) or
  * PBT_PREC_FF (the solve in float-float arithmetic on the FP32 pipes, ~47
- * significant bits; factors must lie below 2^127 in magnitude), anything else
- * PBT_EUNSUPPORTED.  Returns PBT_ESINGULAR (with nothing created) if a zero
- * pivot is met, PBT_EINVAL for bad sizes (1 <= m <= PBT_MAX_BLOCK, nrow >= 2). */
+ * significant bits; factors must lie below 2^127 in magnitude, else
+ * PBT_ERANGE), anything else PBT_EUNSUPPORTED.  Returns PBT_ESINGULAR (with
+ * nothing created) if a zero pivot is met, PBT_EINVAL for bad sizes
+ * (1 <= m <= PBT_MAX_BLOCK, nrow >= 2). */
 int pbt_shared_create(pbt_shared** s, int m, int nrow, const double* a, const double* b, const double* c,
                       int precision);
 
@@ -56,6 +57,13 @@ int pbt_shared_create(pbt_shared** s, int m, int nrow, const double* a, const do
  * solve uses x as its scratch: rows of x hold intermediate values until the
  * backward sweep overwrites them.  Asynchronous on `stream`. */
 int pbt_shared_solve(const pbt_shared* s, const double* rhs, double* x, const pbt_lines* lines, void* stream);
+
+/* Synchronises `stream` and reports the range check of the float-float
+ * solves since the previous call (the rules of pbt_precision in pbt.h: a
+ * right-hand-side value outside 2^-96 <= |x| < 2^96, an overflow, or a line
+ * whose solution lies wholly below 2^-100): PBT_ERANGE if any line failed
+ * (its solution is not valid), else PBT_OK.  Always PBT_OK for FP64. */
+int pbt_shared_status(const pbt_shared* s, void* stream);
 
 /* Block size and rows of the matrix. */
 int pbt_shared_shape(const pbt_shared* s, int* m, int* nrow);

@@ -66,6 +66,16 @@ class DeviceWaitTimeout(RuntimeError):
     """A kernel's bounded wait for its staged input ran out; the solve's result is not valid."""
 
 
+class ArithmeticRangeError(ArithmeticError):
+    """A float-float or FP32 solve left its arithmetic's range (an input outside
+    2^-96 <= |x| < 2^96, an overflow, or a solution below 2^-100); the solution
+    is not valid -- solve with precision "fp64"."""
+
+
+class RefinementNotConverged(ArithmeticError):
+    """The FP32-refined solve did not reach its tolerance in max_iter FP32 solves."""
+
+
 def _raise(code: int, where: str) -> None:
     if code == N.PBT_OK:
         return
@@ -84,6 +94,10 @@ def _raise(code: int, where: str) -> None:
         raise SingularBlockError(msg)
     if code == N.PBT_ETIMEOUT:
         raise DeviceWaitTimeout(msg)
+    if code == N.PBT_ERANGE:
+        raise ArithmeticRangeError(msg)
+    if code == N.PBT_ENOCONV:
+        raise RefinementNotConverged(msg)
     raise RuntimeError(f"{where}: status {code}: {N.last_error()}")
 
 
@@ -185,7 +199,9 @@ class BtdmaGpuPlan:
         return int(N.lib().pbt_plan_workspace_bytes(self._handle)) if self.created else 0
 
     def status(self) -> int:
-        """Synchronise and return the number of zero pivots met since the last call."""
+        """Synchronise and return the number of zero pivots met since the last
+        call; raises DeviceWaitTimeout, ArithmeticRangeError or
+        RefinementNotConverged for those outcomes (pbt_plan_status)."""
         n = C.c_longlong(0)
         code = N.lib().pbt_plan_status(self._handle, C.byref(n))
         if code not in (N.PBT_OK, N.PBT_ESINGULAR):

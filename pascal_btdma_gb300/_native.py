@@ -21,6 +21,8 @@ PBT_EUNSUPPORTED = 4
 PBT_ENOMEM = 5
 PBT_ESINGULAR = 6
 PBT_ETIMEOUT = 7
+PBT_ERANGE = 8
+PBT_ENOCONV = 9
 
 PBT_PREC_FP64 = 0
 PBT_PREC_FF = 1
@@ -99,10 +101,6 @@ SIGNATURES = {
     "pbt_version": (C.c_int, []),
 }
 
-PROBE_SIGNATURES = {
-    "pbt_probe_fma_rates": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
-}
-
 SYNTH_SIGNATURES = {
     "pbt_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "pbt_synth_uniform": (C.c_double, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
@@ -143,7 +141,7 @@ def lib() -> C.CDLL:
     """The loaded libpbt.so (raises if it has not been built)."""
     global _lib
     if _lib is None:
-        _lib = _bind(LIB_PATH, {**SIGNATURES, **PROBE_SIGNATURES})
+        _lib = _bind(LIB_PATH, SIGNATURES)
     return _lib
 
 

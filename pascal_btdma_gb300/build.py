@@ -6,6 +6,8 @@ Outputs (git-ignored, rebuilt on the GPU host because it is a different CPU
 architecture):
     pascal_btdma_gb300/libpbt.so        CUDA kernels + C ABI (include/pbt.h), sm_103a
     pascal_btdma_gb300/libpbt_synth.so  synthetic workload generator (include/pbt_synth.h)
+    pascal_btdma_gb300/libpbt_probe.so  FMA-rate probe of the benchmark (probe/fma_probe.cu;
+                                        measurement tooling, not part of libpbt.so)
 
 The FP64 kernel file is compiled once per block size (-DPBT_M=1..10) so the
 unrolled variants compile in parallel; objects are cached under _build/ and
@@ -27,6 +29,8 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libpbt.so"
 SYNTH = PKG / "libpbt_synth.so"
+PROBE = PKG / "libpbt_probe.so"
+PROBE_SRC = PKG / "probe" / "fma_probe.cu"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"] + ARCH
@@ -34,7 +38,7 @@ MAX_BLOCK = 10
 
 # Families of kernels instantiated per block size: (source, object stem).
 PER_M_SOURCES = [("pbt_inst.cu", "F64"), ("pbt_inst.cu", "FF"), ("pbt_inst.cu", "F32")]
-HOST_SOURCES = ["pbt_api.cpp", "pbt_probe.cu", "pbt_noalloc.cu", "pbt_batch.cpp", "pbt_batch_f64.cu",
+HOST_SOURCES = ["pbt_api.cpp", "pbt_noalloc.cu", "pbt_batch.cpp", "pbt_batch_f64.cu",
                 "pbt_batch_ff.cu", "pbt_layout.cu", "pbt_shared.cu"]
 
 
@@ -62,8 +66,15 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"build command failed ({res.returncode}):\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
 
 
+def build_probe() -> Path:
+    """Compile libpbt_probe.so (the benchmark's FMA-rate probe) if its source changed."""
+    if _stale(PROBE, [PROBE_SRC]):
+        _run([_nvcc(), *NVCC_FLAGS, "-shared", "-o", str(PROBE), str(PROBE_SRC), "-cudart", "static"])
+    return PROBE
+
+
 def build(verbose: bool = False, jobs: int | None = None) -> Path:
-    """Compile libpbt.so and libpbt_synth.so if any input changed."""
+    """Compile libpbt.so, libpbt_synth.so and libpbt_probe.so if any input changed."""
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
     hdrs = _headers()
@@ -83,13 +94,13 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         if _stale(obj, [CSRC / src] + hdrs + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))):
             tasks.append((obj, [nvcc, *NVCC_FLAGS, "-x", "cu", "-c", str(CSRC / src), "-o", str(obj)]))
     jobs = jobs or max(2, os.cpu_count() or 2)
-    if tasks:
-        with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
-            futs = {ex.submit(_run, cmd): obj for obj, cmd in tasks}
-            for f in cf.as_completed(futs):
-                f.result()
-                if verbose:
-                    print("built", futs[f].name, flush=True)
+    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
+        futs = {ex.submit(_run, cmd): obj for obj, cmd in tasks}
+        futs[ex.submit(build_probe)] = PROBE
+        for f in cf.as_completed(futs):
+            f.result()
+            if verbose:
+                print("built", futs[f].name, flush=True)
     if tasks or _stale(LIB, objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-cudart", "static"])
     synth_src = CSRC / "pbt_synth.c"

@@ -15,6 +15,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -74,6 +75,7 @@ struct pbt_plan {
     unsigned* rstat = nullptr;
     int last_iters = 0;
     double last_correction = 0.0;
+    int refine_fail = PBT_OK;  // a refined solve that failed, until pbt_plan_status reports it
     size_t bytes = 0;
     cudaStream_t last_stream = nullptr;
     unsigned magic = 0x50425450u;  // "PBTP"
@@ -89,12 +91,13 @@ int check_plan(const pbt_plan* p) {
     return PBT_OK;
 }
 
-int pick_tpb(const pbt_plan_desc& d, int work_items) {
-    if (d.threads_per_block > 0) return d.threads_per_block;
+int pick_tpb(const pbt_plan* p, int work_items) {
+    if (p->desc.threads_per_block > 0) return p->desc.threads_per_block;
     // Enough CTAs to cover every SM when the batch is small: the FP64 pipe is
     // the bound, so one warp per SM already saturates it.
+    const int sms = p->sms > 0 ? p->sms : 1;
     int tpb = 128;
-    while (tpb > 32 && (work_items + tpb - 1) / tpb < 2 * 152) tpb /= 2;
+    while (tpb > 32 && ((long long)work_items + tpb - 1) / tpb < 2LL * sms) tpb /= 2;
     return tpb;
 }
 
@@ -350,6 +353,9 @@ PBT_DISPATCH(run_reduced, launch_reduced)
 PBT_DISPATCH(run_reduced_cyclic, launch_reduced_cyclic)
 PBT_DISPATCH(run_update, launch_update)
 
+// The local-stage and update launches put the segments in gridDim.y.
+constexpr int kMaxSegments = 65535;
+
 int validate(const pbt_plan_desc& d) {
     char buf[256];
     if (d.m < 1 || d.m > PBT_MAX_BLOCK) {
@@ -360,9 +366,10 @@ int validate(const pbt_plan_desc& d) {
         std::snprintf(buf, sizeof buf, "plan: requires nsys > 0 and nrow >= 2 (nsys=%d, nrow=%d)", d.nsys, d.nrow);
         return fail(PBT_EINVAL, buf);
     }
-    if (d.nseg < 1 || d.nrow < 2 * d.nseg) {
-        std::snprintf(buf, sizeof buf, "plan: nseg=%d must be >= 1 with at least 2 rows per segment (nrow=%d)",
-                      d.nseg, d.nrow);
+    if (d.nseg < 1 || d.nseg > kMaxSegments || d.nrow < 2 * d.nseg) {
+        std::snprintf(buf, sizeof buf,
+                      "plan: nseg=%d must be in 1..%d with at least 2 rows per segment (nrow=%d)", d.nseg,
+                      kMaxSegments, d.nrow);
         return fail(PBT_EINVAL, buf);
     }
     if (d.nseg > 1 && d.nrow < 3 * d.nseg) {
@@ -467,7 +474,7 @@ pbt::SolveArgs make_args(pbt_plan* p, double* a, double* b, double* c, double* d
     g.nsys = p->desc.nsys;
     g.nrow = p->desc.nrow;
     g.nseg = p->desc.nseg;
-    g.tpb = pick_tpb(p->desc, work_items);
+    g.tpb = pick_tpb(p, work_items);
     g.stream = s;
     return g;
 }
@@ -531,6 +538,7 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
     p->last_correction = 1.0;
     const pbt::SolveArgs g64 = make_args(p, a, b, c, rhs, s, ds.nsys);
     double prev_ratio = 1.0;
+    bool converged = false;
     for (int it = 1; it < ds.max_iter; ++it) {
         if ((e = cudaMemsetAsync(p->rstat, 0, sizeof(unsigned), s)) != cudaSuccess)
             return cuda_fail(e, "refined solve: statistic reset");
@@ -568,9 +576,15 @@ int solve_refined(pbt_plan* p, double* a, double* b, double* c, double* d, cudaS
         // Stop when the estimated error left after this correction,
         // ratio * rho with the contraction rho = ratio / previous ratio, is
         // below tol.
-        if ((double)ratio * ((double)ratio / prev_ratio) <= ds.tol) break;
+        if ((double)ratio * ((double)ratio / prev_ratio) <= ds.tol) {
+            converged = true;
+            break;
+        }
         prev_ratio = ratio > 0.f ? (double)ratio : 1e-300;
     }
+    // Reported by pbt_plan_status: a correction that came out Inf/NaN (the
+    // FP32 solve could not carry the system), or tol not reached.
+    if (!converged) p->refine_fail = std::isfinite(p->last_correction) ? PBT_ENOCONV : PBT_ERANGE;
     return PBT_OK;
 }
 
@@ -654,18 +668,22 @@ int solve_core(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
         if (!cyclic && p->sub) {
             // The reduced rows are raw values of the arithmetic; the sub-plan
             // reads and writes FP64, so float-float pairs are widened first
-            // and the reduced solution split back after.
+            // and the reduced solution split back after (with the line's
+            // range check).  The blocks' entries below the float-float input
+            // window -- A' and C' decay along long segments -- are zeroed on
+            // the way: negligible next to the identity diagonal blocks, they
+            // would otherwise read as out of range in the float-float sub-plan.
             const bool ff = arith_of(ds.precision) == kFF;
             const size_t rr = (size_t)nsys * 2 * ds.nseg;
             if (ff) {
-                if ((e = pbt::launch_ff_raw_f64(p->ra, rr * m * m, 1, s)) != cudaSuccess ||
-                    (e = pbt::launch_ff_raw_f64(p->rc, rr * m * m, 1, s)) != cudaSuccess ||
+                if ((e = pbt::launch_ff_raw_f64(p->ra, rr * m * m, 2, s)) != cudaSuccess ||
+                    (e = pbt::launch_ff_raw_f64(p->rc, rr * m * m, 2, s)) != cudaSuccess ||
                     (e = pbt::launch_ff_raw_f64(p->rd, rr * m, 1, s)) != cudaSuccess)
                     return cuda_fail(e, "reduced system to FP64");
             }
             rc = solve_core(p->sub, p->ra, p->rb, p->rc, p->rd, m, nsys, 2 * ds.nseg, false, nullptr, s);
             if (rc) return rc;
-            if (ff && (e = pbt::launch_ff_raw_f64(p->rd, rr * m, 0, s)) != cudaSuccess)
+            if (ff && (e = pbt::launch_reduced_to_ff(p->rd, nsys, 2 * ds.nseg, m, p->status, s)) != cudaSuccess)
                 return cuda_fail(e, "reduced solution to float-float");
         } else {
             e = cyclic ? run_reduced_cyclic(arith_of(ds.precision), m, g2) : run_reduced(arith_of(ds.precision), m, g2);
@@ -907,25 +925,40 @@ int pbt_plan_status(pbt_plan* p, long long* nsingular) {
     if (rc) return rc;
     cudaError_t e = cudaStreamSynchronize(p->last_stream);
     if (e != cudaSuccess) return cuda_fail(e, "plan_status: stream synchronize");
-    // The plan's status word and those of its reduced-system plans.
-    unsigned long long v = 0;
+    // The plan's status word and those of its reduced-system plans (layout
+    // in pbt_internal.h), and the host-side outcome of the refined solve.
+    unsigned long long pivots = 0, stalls = 0;
+    bool range = false;
     for (pbt_plan* q = p; q != nullptr; q = q->sub) {
         unsigned long long w = 0;
         e = cudaMemcpy(&w, q->status, sizeof w, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "plan_status: read");
         e = cudaMemset(q->status, 0, sizeof w);
         if (e != cudaSuccess) return cuda_fail(e, "plan_status: reset");
-        v += w;
+        pivots += w & pbt::kPivotCountMask;
+        range |= (w & pbt::kRangeMark) != 0;
+        stalls += w / pbt::kStallMark;
     }
-    const unsigned long long stalls = v / pbt::kStallMark;
-    v %= pbt::kStallMark;
-    if (nsingular) *nsingular = (long long)v;
+    const int refine = p->refine_fail;
+    p->refine_fail = PBT_OK;
+    if (nsingular) *nsingular = (long long)pivots;
     if (stalls) {
         char buf[160];
         std::snprintf(buf, sizeof buf, "%llu bounded device wait(s) ran out; the solution is not valid", stalls);
         return fail(PBT_ETIMEOUT, buf);
     }
-    if (v) return fail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
+    if (range || refine == PBT_ERANGE)
+        return fail(PBT_ERANGE, "a float-float / FP32 value left the arithmetic's range (an input outside "
+                                "2^-96 <= |x| < 2^96, an overflow, or a solution below 2^-100); the solution is "
+                                "not valid: solve with PBT_PREC_FP64");
+    if (pivots) return fail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
+    if (refine == PBT_ENOCONV) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf,
+                      "the refined solve did not reach tol = %.3g in %d FP32 solves (last correction %.3g)",
+                      p->desc.tol, p->last_iters, p->last_correction);
+        return fail(PBT_ENOCONV, buf);
+    }
     return PBT_OK;
 }
 
@@ -956,15 +989,14 @@ int pbt_adjoint_noncyclic(pbt_plan* p, const double* a, const double* b, const d
     adj.dc = dc;
     const int arith = arith_of(ds.precision);
     cudaError_t e;
-    if (p->thomas && ds.m <= 6) {
+    if (p->thomas) {
         e = run_adjoint(arith, m, make_args(p, const_cast<double*>(a), const_cast<double*>(b),
                                             const_cast<double*>(c), g, s, ds.nsys), adj);
         if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
         return PBT_OK;
     }
-    // Segmented plans, and m >= 7 (whose fused FP64 variant gives wrong
-    // results in the rolled-loop build: it is not used): materialise M^T and
-    // solve it with the plan's own forward method.
+    // Segmented plans: materialise M^T and solve it with the plan's own
+    // forward method.
     if (!p->at) {
         const size_t n = (size_t)ds.m * ds.m * ds.nsys * ds.nrow;
         if ((rc = alloc(p, &p->at, n)) || (rc = alloc(p, &p->bt, n)) || (rc = alloc(p, &p->ct, n))) return rc;

@@ -349,10 +349,14 @@ int pbt_batch_status(pbt_batch* b, long long* nsingular, int* timed_out) {
         (e = cudaMemcpy(&err, b->state + 2, sizeof err, cudaMemcpyDeviceToHost)) != cudaSuccess ||
         (e = cudaMemset(b->status, 0, sizeof v)) != cudaSuccess)
         return bcuda(e, "batch_status: read");
-    if (nsingular) *nsingular = (long long)v;
+    const unsigned long long pivots = v & pbt::kPivotCountMask;
+    if (nsingular) *nsingular = (long long)pivots;
     if (timed_out) *timed_out = err;
     if (err) return bfail(PBT_ECUDA, "batch_status: a wait of the persistent kernel ran out; the result is invalid");
-    if (v) return bfail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
+    if (v & pbt::kRangeMark)
+        return bfail(PBT_ERANGE, "a float-float value left the arithmetic's range (an input outside "
+                                 "2^-96 <= |x| < 2^96, an overflow, or a solution below 2^-100); the result is invalid");
+    if (pivots) return bfail(PBT_ESINGULAR, "a zero pivot was met in at least one block");
     return PBT_OK;
 }
 

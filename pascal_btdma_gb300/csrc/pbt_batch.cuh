@@ -46,7 +46,7 @@ __host__ __device__ constexpr bool batch_uses_lu() {
 constexpr int kBatchLuSlots = 5 * 5 + 5;
 
 template <class Num, int M>
-__device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTile& tl, int t, int seg, bool& bad) {
+__device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTile& tl, int t, int seg, unsigned& bad) {
     const int lane = threadIdx.x & 31;
     const size_t plane = (size_t)32 * tl.rows, rs = 32;
     const int n_lane = ba.lane_rows[t * 32 + lane];
@@ -92,7 +92,7 @@ __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTil
 }
 
 template <class Num, int M>
-__device__ __forceinline__ void batch_stage3(const BatchArgs& ba, const BatchTile& tl, int t, int seg) {
+__device__ __forceinline__ void batch_stage3(const BatchArgs& ba, const BatchTile& tl, int t, int seg, unsigned& bad) {
     const int lane = threadIdx.x & 31;
     const size_t plane = (size_t)32 * tl.rows, rs = 32;
     const int n_lane = ba.lane_rows[t * 32 + lane];
@@ -101,8 +101,10 @@ __device__ __forceinline__ void batch_stage3(const BatchArgs& ba, const BatchTil
     int f, l;
     seg_rows(n_lane, tl.nseg, seg, f, l);
     const size_t fo = (size_t)f * rs;
+    unsigned amax = 0;
     update_body<Num, M>(ba.aw + mo + fo, ba.cw + mo + fo, ba.d + vo + fo, plane, rs, l - f + 1, true,
-                        ba.rd + tl.red_vec_off + lane, (size_t)32 * 2 * tl.nseg, rs, seg);
+                        ba.rd + tl.red_vec_off + lane, (size_t)32 * 2 * tl.nseg, rs, seg, amax);
+    bad |= range_bits<Num>(amax, false);
 }
 
 // Block sizes of the batch kernel: 1..kBatchMaxBlock (the host refuses
@@ -119,7 +121,7 @@ constexpr int kBatchMaxBlock = 5;
 
 template <class Num>
 __global__ void __launch_bounds__(128) k_batch(const BatchArgs ba) {
-    bool bad = false;
+    unsigned bad = 0;
     // Stage 1 (and the reduced solves).
     while (true) {
         const int item = warp_claim(ba.head1);
@@ -151,11 +153,11 @@ __global__ void __launch_bounds__(128) k_batch(const BatchArgs ba) {
         if (!ok) break;
         __threadfence();
         const BatchTile tl = ba.tiles[it.x];
-#define PBT_S3(MM) batch_stage3<Num, MM>(ba, tl, it.x, it.y)
+#define PBT_S3(MM) batch_stage3<Num, MM>(ba, tl, it.x, it.y, bad)
         PBT_BATCH_SWITCH(PBT_S3)
 #undef PBT_S3
     }
-    if (bad) atomicAdd(ba.status, 1ull);
+    report_status(ba.status, bad);
 }
 
 // Packing between the caller's per-system layout (system s at its own

@@ -58,9 +58,13 @@ struct ThomasMaps {
 // Largest block size with a staged kernel (larger blocks do not fit in the
 // registers of one thread anyway and keep the direct-load kernel).
 constexpr int kStagedMaxBlock = 6;
-// Added to a plan's status word (which otherwise counts zero pivots) by a
-// kernel whose bounded wait ran out.
+// A plan's status word: bits 0..46 count the threads that met a zero pivot,
+// bit 47 is set (atomicOr) by a thread whose float-float / FP32 solution left
+// the arithmetic's range, and kStallMark is added once per bounded wait that
+// ran out.
 constexpr unsigned long long kStallMark = 1ull << 48;
+constexpr unsigned long long kRangeMark = 1ull << 47;
+constexpr unsigned long long kPivotCountMask = kRangeMark - 1;
 
 // Kernel launchers, explicitly instantiated per arithmetic and block size M
 // (1..PBT_MAX_BLOCK) in pbt_inst.cu.  Each returns cudaGetLastError().
@@ -107,8 +111,12 @@ template <int M> cudaError_t launch_refine_staged(const SolveArgs& g, const Thom
 // Layout conversion for PBT_FLAG_CPU_LAYOUT plans (pbt_layout.cu): E elements
 // per (system, row); dir 0: CPU layout src -> GPU layout dst, 1: back.
 cudaError_t launch_layout(const double* src, double* dst, int E, int nsys, int nrow, int dir, cudaStream_t s);
-// In place, n 8-byte slots: raw float-float pairs -> FP64 (to_f64 = 1) or back.
+// In place, n 8-byte slots: raw float-float pairs -> FP64 (to_f64 = 1; 2
+// also zeroes values below 2^-96) or back (0).
 cudaError_t launch_ff_raw_f64(double* x, size_t n, int to_f64, cudaStream_t s);
+// The reduced solution rd (nsys systems, `rows` rows of m values) from FP64
+// back to raw float-float pairs, with the line's range check into `status`.
+cudaError_t launch_reduced_to_ff(double* rd, int nsys, int rows, int m, unsigned long long* status, cudaStream_t s);
 
 // Records the message returned by pbt_last_error_string() on this thread and
 // returns `code` (defined in pbt_api.cpp).

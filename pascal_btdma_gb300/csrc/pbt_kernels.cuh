@@ -33,6 +33,8 @@
 // caller's A and C are converted to FP64 so those arrays stay valid doubles.
 #pragma once
 
+#include <math_constants.h>
+
 #include <type_traits>
 
 #include "pbt_util.cuh"
@@ -70,7 +72,7 @@ __device__ __forceinline__ void seg_rows(int n, int p, int s, int& first, int& l
 // arithmetic goes on (Inf/NaN), like the reference.
 // ---------------------------------------------------------------------------
 template <class Num, int M, int NR>
-__device__ __forceinline__ void gesv(typename Num::Acc (&a)[M][M], typename Num::Acc (&b)[M][NR], bool& bad) {
+__device__ __forceinline__ void gesv(typename Num::Acc (&a)[M][M], typename Num::Acc (&b)[M][NR], unsigned& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
     T rinv[M];
@@ -164,7 +166,7 @@ struct LU {
 };
 
 template <class Num, int M>
-__device__ __forceinline__ void lu_factor(typename Num::Acc (&a)[M][M], LU<Num, M>& lu, bool& bad) {
+__device__ __forceinline__ void lu_factor(typename Num::Acc (&a)[M][M], LU<Num, M>& lu, unsigned& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
 PBT_UNROLL
@@ -286,11 +288,18 @@ __device__ __forceinline__ void st_raw_vec(double* base, size_t plane, const typ
 PBT_UNROLL
     for (int i = 0; i < M; ++i) Num::sts(base + (size_t)i * plane, x[i]);
 }
+// Solution values: converted to FP64 on store, their largest magnitude
+// (Num::mag, an ordered integer with Inf/NaN above every finite value)
+// collected in `amax` for range_bits.
 template <class Num, int M>
-__device__ __forceinline__ void out_vec(double* base, size_t plane, const typename Num::T (&x)[M]) {
+__device__ __forceinline__ void out_vec(double* base, size_t plane, const typename Num::T (&x)[M], unsigned& amax) {
 PBT_UNROLL
-    for (int i = 0; i < M; ++i) Num::out(base + (size_t)i * plane, x[i]);
+    for (int i = 0; i < M; ++i) {
+        Num::out(base + (size_t)i * plane, x[i]);
+        amax = max(amax, Num::mag(x[i]));
+    }
 }
+
 // Factor storage: raw in the plan's workspace, FP64 when written in place.
 template <class Num, int M>
 __device__ __forceinline__ void st_fac_blk(double* base, size_t plane, const typename Num::T (&x)[M][M], bool raw) {
@@ -349,10 +358,11 @@ constexpr int kThomasThreads = PBT_THOMAS_THREADS;
 // stride (the number of systems interleaved in the layout).
 template <class Num, int M>
 __device__ __forceinline__ void thomas_body(const double* A, const double* B, const double* C, double* D,
-                                            double* CW, size_t plane0, size_t rs, int N, bool raw, bool& bad) {
+                                            double* CW, size_t plane0, size_t rs, int N, bool raw, unsigned& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
     T cp[M][M], y[M];
+    unsigned amax = 0;
     for (int q = 0; q < N; ++q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
@@ -365,7 +375,7 @@ PBT_UNROLL
 PBT_UNROLL
                 for (int k = 0; k < M; ++k) ar[k] = Num::in(A + o + (size_t)(i + M * k) * plane);
             }
-            Acc t = Num::acc(Num::in(D + o + (size_t)i * plane));
+            Acc t = Num::acc(Num::in_rhs(D + o + (size_t)i * plane));
             if (q > 0) {
 PBT_UNROLL
                 for (int k = 0; k < M; ++k) Num::msub(t, ar[k], y[k]);
@@ -403,7 +413,7 @@ PBT_UNROLL
             gesv<Num, M, 1>(r, xv, bad);
 PBT_UNROLL
             for (int i = 0; i < M; ++i) y[i] = Num::fin(xv[i][0]);
-            out_vec<Num, M>(D + o, plane, y);
+            out_vec<Num, M>(D + o, plane, y, amax);
         }
     }
     for (int q = N - 2; q >= 0; --q) {
@@ -421,8 +431,9 @@ PBT_UNROLL
         }
 PBT_UNROLL
         for (int i = 0; i < M; ++i) y[i] = t[i];
-        out_vec<Num, M>(D + o, plane, y);
+        out_vec<Num, M>(D + o, plane, y, amax);
     }
+    bad |= range_bits<Num>(amax, true);
 }
 
 // Which body the direct-load single-segment kernel runs per block size:
@@ -489,7 +500,7 @@ __host__ __device__ constexpr bool thomas_uses_lu() {
 template <class Num, int M>
 __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B, const double* C, double* D,
                                                double* CW, double* cps, int cstride, size_t plane0, size_t rs,
-                                               int N, bool raw, bool& bad) {
+                                               int N, bool raw, unsigned& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
     // Element e = i + M*j of a row's block is at base + e*plane: every phase
@@ -497,6 +508,7 @@ __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B,
     // the plane stride through opaque() so that no phase keeps a table of
     // 64-bit element addresses alive across the arithmetic.
     T y[M];
+    unsigned amax = 0;
     for (int q = 0; q < N; ++q) {
         const size_t o = (size_t)q * rs;
         const bool last = (q == N - 1);
@@ -505,7 +517,7 @@ __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B,
             const size_t plane = opaque(plane0);
             const double* pd = D + o;
 PBT_UNROLL
-            for (int i = 0; i < M; ++i, pd += plane) xd[i] = Num::acc(Num::in(pd));
+            for (int i = 0; i < M; ++i, pd += plane) xd[i] = Num::acc(Num::in_rhs(pd));
         }
         {
             const size_t plane = opaque(plane0);
@@ -570,7 +582,7 @@ PBT_UNROLL
         {
             const size_t plane = opaque(plane0);
             if (last) {
-                out_vec<Num, M>(D + o, plane, y);
+                out_vec<Num, M>(D + o, plane, y, amax);
                 break;
             }
             st_raw_vec<Num, M>(D + o, plane, y);
@@ -637,8 +649,9 @@ PBT_UNROLL
         }
 PBT_UNROLL
         for (int i = 0; i < M; ++i) y[i] = t[i];
-        out_vec<Num, M>(D + o, plane, y);
+        out_vec<Num, M>(D + o, plane, y, amax);
     }
+    bad |= range_bits<Num>(amax, true);
 }
 
 
@@ -646,7 +659,7 @@ template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
     if (sys >= g.nsys) return;
-    bool bad = false;
+    unsigned bad = 0;
     if constexpr (thomas_uses_lu<M>()) {
         extern __shared__ double thomas_cps[];
         thomas_body_lu<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, thomas_cps + threadIdx.x,
@@ -656,7 +669,7 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
         thomas_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
                             (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
     }
-    if (bad) atomicAdd(g.status, 1ull);
+    report_status(g.status, bad);
 }
 
 // The same solve for lines addressed by strides (pbt_solve_noncyclic_lines).
@@ -668,7 +681,7 @@ template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_lines(const SolveArgs g, const LineStrides ls) {
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
     if (sys >= g.nsys) return;
-    bool bad = false;
+    unsigned bad = 0;
     const size_t o = (size_t)(sys % ls.lin) * (size_t)ls.in + (size_t)(sys / ls.lin) * (size_t)ls.out;
     if constexpr (thomas_uses_lu<M>()) {
         extern __shared__ double thomas_cps[];
@@ -678,7 +691,7 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_lines(const SolveArgs g
         thomas_body<Num, M>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, (size_t)ls.elem, (size_t)ls.row, g.nrow,
                             g.factors_raw != 0, bad);
     }
-    if (bad) atomicAdd(g.status, 1ull);
+    report_status(g.status, bad);
 }
 
 // ---------------------------------------------------------------------------
@@ -689,7 +702,7 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_lines(const SolveArgs g
 template <class Num, int M>
 __device__ __forceinline__ void modi_body(const double* A, const double* B, const double* C, double* D, double* AW,
                                           double* CW, size_t plane0, size_t rs, int n, bool raw, double* RA,
-                                          double* RC, double* RD, size_t rplane, size_t rrs, int seg, bool& bad) {
+                                          double* RC, double* RD, size_t rplane, size_t rrs, int seg, unsigned& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
 
@@ -706,7 +719,7 @@ PBT_UNROLL
             T ar[M];
 PBT_UNROLL
             for (int k = 0; k < M; ++k) ar[k] = Num::in(A + o + (size_t)(i + M * k) * plane);
-            Acc t = Num::acc(Num::in(D + o + (size_t)i * plane));
+            Acc t = Num::acc(Num::in_rhs(D + o + (size_t)i * plane));
             if (!first2) {
 PBT_UNROLL
                 for (int k = 0; k < M; ++k) Num::msub(t, ar[k], dp[k]);
@@ -874,10 +887,10 @@ __global__ void __launch_bounds__(128) k_modi(const SolveArgs g) {
     seg_rows(g.nrow, g.nseg, seg, f, l);
     const size_t rs = (size_t)g.nsys;
     const size_t fo = (size_t)f * rs + sys;
-    bool bad = false;
+    unsigned bad = 0;
     modi_body<Num, M>(g.a + fo, g.b + fo, g.c + fo, g.d + fo, g.aw + fo, g.cw + fo, rs * g.nrow, rs, l - f + 1,
                       g.factors_raw != 0, g.ra + sys, g.rc + sys, g.rd + sys, rs * 2 * g.nseg, rs, seg, bad);
-    if (bad) atomicAdd(g.status, 1ull);
+    report_status(g.status, bad);
 }
 
 // ---------------------------------------------------------------------------
@@ -886,7 +899,7 @@ __global__ void __launch_bounds__(128) k_modi(const SolveArgs g) {
 // ---------------------------------------------------------------------------
 template <class Num, int M>
 __device__ __forceinline__ void reduced_body(const double* RA, double* RC, double* RD, size_t plane0, size_t rs,
-                                             int R, bool& bad) {
+                                             int R, unsigned& bad) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
 
@@ -940,6 +953,12 @@ PBT_UNROLL
         }
         st_raw_vec<Num, M>(RD + o, plane, y);
     }
+    // The reduced solution (the segments' end rows) stands for the system's
+    // solution in the range check: a whole line below the float-float limit,
+    // or a non-finite value, shows here.
+    unsigned amax = 0;
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) amax = max(amax, Num::mag(y[i]));
     for (int q = R - 2; q >= 0; --q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
@@ -952,21 +971,23 @@ PBT_UNROLL
 PBT_UNROLL
             for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
             t[i] = Num::fin(s);
+            amax = max(amax, Num::mag(t[i]));
         }
 PBT_UNROLL
         for (int i = 0; i < M; ++i) y[i] = t[i];
         st_raw_vec<Num, M>(RD + o, plane, y);
     }
+    bad |= range_bits<Num>(amax, true);
 }
 
 template <class Num, int M>
 __global__ void __launch_bounds__(128) k_reduced(const SolveArgs g) {
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
     if (sys >= g.nsys) return;
-    bool bad = false;
+    unsigned bad = 0;
     const size_t rs = (size_t)g.nsys;
     reduced_body<Num, M>(g.ra + sys, g.rc + sys, g.rd + sys, rs * 2 * g.nseg, rs, 2 * g.nseg, bad);
-    if (bad) atomicAdd(g.status, 1ull);
+    report_status(g.status, bad);
 }
 
 // ---------------------------------------------------------------------------
@@ -987,7 +1008,7 @@ __global__ void __launch_bounds__(128) k_reduced_cyclic(const SolveArgs g) {
     double* RC = g.rc + sys;
     double* RD = g.rd + sys;
     double* RE = g.re + sys;
-    bool bad = false;
+    unsigned bad = 0;
 
     // Row 1: B = I, so [d'|e'|c'] = [d | -A_1 | C_1] exactly.
     T cp[M][M], ep[M][M], dp[M];
@@ -1117,7 +1138,10 @@ PBT_UNROLL
         for (int i = 0; i < M; ++i) x0[i] = Num::fin(x[i][0]);
         st_raw_vec<Num, M>(RD, plane0, x0);
     }
-    // Rows 1..R-1: x_q = d'_q + e'_q x_0.
+    // Rows 1..R-1: x_q = d'_q + e'_q x_0; the range check as in reduced_body.
+    unsigned amax = 0;
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) amax = max(amax, Num::mag(x0[i]));
     for (int q = 1; q < R; ++q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
@@ -1130,10 +1154,12 @@ PBT_UNROLL
 PBT_UNROLL
             for (int k = 0; k < M; ++k) Num::mac(s, e[i][k], x0[k]);
             t[i] = Num::fin(s);
+            amax = max(amax, Num::mag(t[i]));
         }
         st_raw_vec<Num, M>(RD + o, plane, t);
     }
-    if (bad) atomicAdd(g.status, 1ull);
+    bad |= range_bits<Num>(amax, true);
+    report_status(g.status, bad);
 }
 
 // ---------------------------------------------------------------------------
@@ -1141,14 +1167,15 @@ PBT_UNROLL
 // ---------------------------------------------------------------------------
 template <class Num, int M>
 __device__ __forceinline__ void update_body(const double* AW, const double* CW, double* D, size_t plane0, size_t rs,
-                                            int n, bool raw, const double* RD, size_t rplane, size_t rrs, int seg) {
+                                            int n, bool raw, const double* RD, size_t rplane, size_t rrs, int seg,
+                                            unsigned& amax) {
     using T = typename Num::T;
     using Acc = typename Num::Acc;
     T x0[M], xn[M];
     ld_raw_vec<Num, M>(x0, RD + rrs * (size_t)(2 * seg), rplane);
     ld_raw_vec<Num, M>(xn, RD + rrs * (size_t)(2 * seg + 1), rplane);
-    out_vec<Num, M>(D, plane0, x0);
-    out_vec<Num, M>(D + (size_t)(n - 1) * rs, plane0, xn);
+    out_vec<Num, M>(D, plane0, x0, amax);
+    out_vec<Num, M>(D + (size_t)(n - 1) * rs, plane0, xn, amax);
     for (int q = 1; q < n - 1; ++q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
@@ -1165,7 +1192,7 @@ PBT_UNROLL
             for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], xn[k]);
             t[i] = Num::fin(s);
         }
-        out_vec<Num, M>(D + o, plane, t);
+        out_vec<Num, M>(D + o, plane, t, amax);
     }
 }
 
@@ -1178,8 +1205,12 @@ __global__ void __launch_bounds__(128) k_update(const SolveArgs g) {
     seg_rows(g.nrow, g.nseg, seg, f, l);
     const size_t rs = (size_t)g.nsys;
     const size_t fo = (size_t)f * rs + sys;
+    unsigned amax = 0;
     update_body<Num, M>(g.aw + fo, g.cw + fo, g.d + fo, rs * g.nrow, rs, l - f + 1, g.factors_raw != 0, g.rd + sys,
-                        rs * 2 * g.nseg, rs, seg);
+                        rs * 2 * g.nseg, rs, seg, amax);
+    // One segment of a line: Inf/NaN only (the reduced solve checked the
+    // line's magnitude).
+    report_status(g.status, range_bits<Num>(amax, false));
 }
 
 // ---------------------------------------------------------------------------
@@ -1197,6 +1228,40 @@ __global__ void __launch_bounds__(128) k_update(const SolveArgs g) {
 // is reused for the adjoint's own C').  g holds dL/dx on entry and lambda on
 // return; da/db/dc may be null.
 // ---------------------------------------------------------------------------
+// The gradient blocks that row q of the adjoint's backward sweep completes:
+//   dB_q = -lambda_q x_q^T,  dC_q = -lambda_q x_{q+1}^T (0 at the last row),
+//   dA_{q+1} = -lambda_{q+1} x_q^T, and dA_0 = 0 at q = 0,
+// from lambda_q (lq) and lambda_{q+1} (ln, when `next`) as the FP64 values the
+// sweep stores, and x_q, x_{q+1} read from X (this thread's system).  Nothing
+// is carried across rows but the sweep's own y: the first form of this sweep
+// kept lambda_q, lambda_{q+1}, x_q and x_{q+1} in six m-long per-thread arrays,
+// copied and reset together between rows, and its FP64 rolled-loop
+// instantiation (m >= 7) returned a wrong lambda from the last row on -- right
+// when fully unrolled, in float-float, or without those arrays, and unchanged
+// by ptxas -O0 -- so that construct is avoided.
+template <class Num, int M>
+__device__ __forceinline__ void adjoint_gradients(const AdjointArgs& adj, const typename Num::T (&lq)[M],
+                                                  const typename Num::T (&ln)[M], bool next, const double* X,
+                                                  int sys, size_t o, size_t plane, size_t rs, int q) {
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) {
+        const double li = Num::f64(lq[i]);
+        const double lni = next ? Num::f64(ln[i]) : 0.0;
+PBT_UNROLL
+        for (int j = 0; j < M; ++j) {
+            const size_t e = sys + o + (size_t)(i + M * j) * plane;
+            const double xj = __ldg(X + o + (size_t)j * plane);
+            const double xnj = next ? __ldg(X + o + rs + (size_t)j * plane) : 0.0;
+            if (adj.db) adj.db[e] = -li * xj;
+            if (adj.dc) adj.dc[e] = -li * xnj;
+            if (adj.da) {
+                if (next) adj.da[e + rs] = -lni * xj;
+                if (q == 0) adj.da[e] = 0.0;
+            }
+        }
+    }
+}
+
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_adjoint(const SolveArgs g, const AdjointArgs adj) {
     using T = typename Num::T;
@@ -1211,7 +1276,7 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_adjoint(const SolveArgs g, con
     const double* C = g.c + sys;
     double* G = adj.g + sys;
     double* CW = g.cw + sys;
-    bool bad = false;
+    unsigned bad = 0, amax = 0;
 
     // Forward over the transposed rows.
     T cp[M][M], y[M];
@@ -1228,7 +1293,7 @@ PBT_UNROLL
 PBT_UNROLL
                 for (int k = 0; k < M; ++k) ar[k] = Num::in(C + o - rs + (size_t)(k + M * i) * plane);
             }
-            Acc t = Num::acc(Num::in(G + o + (size_t)i * plane));
+            Acc t = Num::acc(Num::in_rhs(G + o + (size_t)i * plane));
             if (q > 0) {
 PBT_UNROLL
                 for (int k = 0; k < M; ++k) Num::msub(t, ar[k], y[k]);
@@ -1269,75 +1334,32 @@ PBT_UNROLL
             for (int i = 0; i < M; ++i) y[i] = Num::fin(xv[i][0]);
         }
     }
-    // Backward: lambda_q = y_q - Ct'_q lambda_{q+1}, with the gradient blocks.
+    // Backward: lambda_q = y_q - Ct'_q lambda_{q+1}; y holds lambda_{q+1} on
+    // entry to row q and lambda_q after it.  The gradient blocks of row q
+    // take lambda_q from t and lambda_{q+1} from y before y is overwritten.
     const double* X = adj.x + sys;
-    double xq[M], xn[M];
-    T lam[M], lamn[M];
-    double lamd[M], lamnd[M];
-PBT_UNROLL
-    for (int i = 0; i < M; ++i) {
-        lam[i] = y[i];
-        xq[i] = X[(size_t)(N - 1) * rs + (size_t)i * plane0];
-        lamn[i] = Num::zero();
-        lamnd[i] = 0.0;
-        xn[i] = 0.0;
-    }
-    for (int q = N - 1; q >= 0; --q) {
+    out_vec<Num, M>(G + (size_t)(N - 1) * rs, plane0, y, amax);
+    adjoint_gradients<Num, M>(adj, y, y, false, X, sys, (size_t)(N - 1) * rs, plane0, rs, N - 1);
+    for (int q = N - 2; q >= 0; --q) {
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
-        if (q < N - 1) {
-            T c[M][M], t[M];
-            ld_raw_blk<Num, M>(c, CW + o, plane);
-            ld_raw_vec<Num, M>(t, G + o, plane);
-PBT_UNROLL
-            for (int i = 0; i < M; ++i) {
-                Acc s = Num::acc(t[i]);
-PBT_UNROLL
-                for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], lamn[k]);
-                lam[i] = Num::fin(s);
-            }
-PBT_UNROLL
-            for (int i = 0; i < M; ++i) xq[i] = X[o + (size_t)i * plane];
-        }
-        out_vec<Num, M>(G + o, plane, lam);
-PBT_UNROLL
-        for (int i = 0; i < M; ++i) lamd[i] = G[o + (size_t)i * plane];
-        // dB_q = -lambda_q x_q^T; dC_q = -lambda_q x_{q+1}^T; dA_{q+1} = -lambda_{q+1} x_q^T
-        if (adj.db) {
-PBT_UNROLL
-            for (int j = 0; j < M; ++j)
-PBT_UNROLL
-                for (int i = 0; i < M; ++i) adj.db[sys + o + (size_t)(i + M * j) * plane] = -lamd[i] * xq[j];
-        }
-        if (adj.dc) {
-PBT_UNROLL
-            for (int j = 0; j < M; ++j)
-PBT_UNROLL
-                for (int i = 0; i < M; ++i)
-                    adj.dc[sys + o + (size_t)(i + M * j) * plane] = (q < N - 1) ? -lamd[i] * xn[j] : 0.0;
-        }
-        if (adj.da) {
-            if (q < N - 1) {
-PBT_UNROLL
-                for (int j = 0; j < M; ++j)
-PBT_UNROLL
-                    for (int i = 0; i < M; ++i) adj.da[sys + o + rs + (size_t)(i + M * j) * plane] = -lamnd[i] * xq[j];
-            }
-            if (q == 0) {
-PBT_UNROLL
-                for (int j = 0; j < M; ++j)
-PBT_UNROLL
-                    for (int i = 0; i < M; ++i) adj.da[sys + (size_t)(i + M * j) * plane] = 0.0;
-            }
-        }
+        T c[M][M], t[M];
+        ld_raw_blk<Num, M>(c, CW + o, plane);
+        ld_raw_vec<Num, M>(t, G + o, plane);
 PBT_UNROLL
         for (int i = 0; i < M; ++i) {
-            lamn[i] = lam[i];
-            lamnd[i] = lamd[i];
-            xn[i] = xq[i];
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+            t[i] = Num::fin(s);
         }
+        out_vec<Num, M>(G + o, plane, t, amax);
+        adjoint_gradients<Num, M>(adj, t, y, true, X, sys, o, plane, rs, q);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) y[i] = t[i];
     }
-    if (bad) atomicAdd(g.status, 1ull);
+    bad |= range_bits<Num>(amax, true);
+    report_status(g.status, bad);
 }
 
 // Segmented adjoint, step 1: materialise M^T's blocks (At, Bt, Ct) in the
@@ -1441,6 +1463,25 @@ PBT_UNROLL
     }
 }
 
+// The refinement's per-system statistic: max|e| and max|x| over a system's
+// correction e and updated solution x; a non-finite x makes max|e| +Inf
+// (fmax would skip a NaN).
+__device__ __forceinline__ void refine_stat(double& emax, double& xmax, double e, double x) {
+    emax = fmax(emax, fabs(e));
+    xmax = fmax(xmax, fabs(x));
+    if ((__double2hiint(x) & 0x7ff00000) == 0x7ff00000) emax = CUDART_INF;
+}
+// One system's convergence statistic max|e| / max|x| (+Inf when undefined or
+// not finite) into *stat, and its range check into the plan's status word: a
+// solution that is not finite, or that lies wholly below 2^-100 (where the
+// FP32 corrections underflow and stop refining it), is a range failure.
+__device__ __forceinline__ void refine_report(double emax, double xmax, unsigned* stat, unsigned long long* status) {
+    float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
+    if (!(ratio == ratio)) ratio = INFINITY;
+    atomicMax(stat, __float_as_uint(ratio));
+    if (!(ratio < INFINITY) || (xmax > 0.0 && xmax < 0x1p-100)) atomicOr(status, kRangeMark);
+}
+
 template <int M>
 __global__ void __launch_bounds__(32 * M) k_accumulate(const SolveArgs g, double* __restrict__ X,
                                                        const double* __restrict__ E, unsigned* stat) {
@@ -1456,8 +1497,7 @@ __global__ void __launch_bounds__(32 * M) k_accumulate(const SolveArgs g, double
             const double e = E[o];
             const double x = X[o] + e;
             X[o] = x;
-            emax = fmax(emax, fabs(e));
-            xmax = fmax(xmax, fabs(x));
+            refine_stat(emax, xmax, e, x);
         }
     }
     red[0][i][lane] = emax;
@@ -1469,10 +1509,7 @@ PBT_UNROLL
             emax = fmax(emax, red[0][k][lane]);
             xmax = fmax(xmax, red[1][k][lane]);
         }
-        // NaN-safe: a non-finite or undefined ratio reports +Inf.
-        float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
-        if (!(ratio == ratio)) ratio = INFINITY;
-        if (sys < g.nsys) atomicMax(stat, __float_as_uint(ratio));
+        if (sys < g.nsys) refine_report(emax, xmax, stat, g.status);
     }
 }
 
@@ -1546,7 +1583,7 @@ PBT_UNROLL
                         r[i] = fma(-__ldg(g.c + sys + o + (size_t)(i + M * k) * plane), xp[k], r[i]);
             }
 PBT_UNROLL
-            for (int i = 0; i < M; ++i) ta[i] = F32::acc(FF::split(r[i]).h);
+            for (int i = 0; i < M; ++i) ta[i] = F32::acc(FF::split_wide(r[i]).h);
             if (q > 0) {
 PBT_UNROLL
                 for (int k = 0; k < M; ++k)
@@ -1598,14 +1635,10 @@ PBT_UNROLL
                 const double ed = FF::widen(e[i]);
                 const double x = *px + ed;
                 *px = x;
-                emax = fmax(emax, fabs(ed));
-                xmax = fmax(xmax, fabs(x));
+                refine_stat(emax, xmax, ed, x);
             }
         }
-        // NaN-safe: a non-finite or undefined ratio reports +Inf.
-        float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
-        if (!(ratio == ratio)) ratio = INFINITY;
-        atomicMax(ra.stat, __float_as_uint(ratio));
+        refine_report(emax, xmax, ra.stat, g.status);
     }
 }
 

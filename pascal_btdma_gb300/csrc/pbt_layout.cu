@@ -86,14 +86,21 @@ __global__ void __launch_bounds__(kThreads) k_layout(const double* __restrict__ 
 
 // In place: raw float-float pairs (8-byte slots, as the kernels keep their
 // intermediates) <-> FP64 values.  The pair (h, l) has |l| <= ulp(h)/2, so
-// h + l is exact in FP64; back, FF::split keeps 47 bits.
+// h + l is exact in FP64; back, FF::split_wide keeps 47 bits (these are the
+// library's own intermediates: no input window).
+// to_f64 = 2 also sets values below the float-float input window (|v| <
+// 2^-96) to zero: used on the reduced system's blocks before a float-float
+// sub-plan reads them as its matrix, where such entries are negligible next
+// to the identity diagonal blocks (A' and C' decay along long segments).
 __global__ void k_ff_raw_f64(double* x, size_t n, int to_f64) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         if (to_f64) {
-            x[i] = FF::join(FF::lds(x + i));
+            const double v = FF::join(FF::lds(x + i));
+            const unsigned e = ((unsigned)__double2hiint(v) >> 20) & 0x7ffu;
+            x[i] = (to_f64 == 2 && e < kFFExpLo) ? 0.0 : v;
         } else {
             const double v = x[i];
-            FF::sts(x + i, FF::split(v));
+            FF::sts(x + i, FF::split_wide(v));
         }
     }
 }
@@ -154,6 +161,39 @@ cudaError_t launch_lines_layout(const double* src, double* dst, const LineStride
     const int nsb = (nsys + 31) / 32;
     const dim3 grid((unsigned)((nrow + 31) / 32), (unsigned)(nsb < 65535 ? nsb : 65535), (unsigned)E);
     k_lines_layout<<<grid, dim3(32, 8), 0, s>>>(src, dst, ls, nsys, nrow, dir);
+    return cudaGetLastError();
+}
+
+// The reduced solution of a float-float plan after its FP64 sub-solve, back
+// to raw pairs (rd[sys + nsys*(r + rows*i)]).  A CTA is 32 systems x 32
+// threads along their values, so that the line's range check (range_bits: a
+// non-finite value, or the whole reduced solution below the float-float
+// limit) sees all of a system's values after one shared-memory reduction.
+__global__ void __launch_bounds__(1024) k_reduced_to_ff(double* rd, int nsys, int rows, int m,
+                                                       unsigned long long* status) {
+    __shared__ unsigned red[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int sys = blockIdx.x * 32 + tx;
+    unsigned amax = 0;
+    if (sys < nsys) {
+        const size_t n = (size_t)rows * m;
+        for (size_t k = ty; k < n; k += 32) {
+            double* p = rd + sys + (size_t)nsys * k;
+            const FF::T v = FF::split_wide(*p);
+            amax = max(amax, FF::mag(v));
+            FF::sts(p, v);
+        }
+    }
+    red[ty][tx] = amax;
+    __syncthreads();
+    if (ty == 0 && sys < nsys) {
+        for (int k = 1; k < 32; ++k) amax = max(amax, red[k][tx]);
+        report_status(status, range_bits<FF>(amax, true));
+    }
+}
+
+cudaError_t launch_reduced_to_ff(double* rd, int nsys, int rows, int m, unsigned long long* status, cudaStream_t s) {
+    k_reduced_to_ff<<<(unsigned)((nsys + 31) / 32), dim3(32, 32), 0, s>>>(rd, nsys, rows, m, status);
     return cudaGetLastError();
 }
 

@@ -20,7 +20,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 
 #include "pbt_internal.h"
 
@@ -32,17 +31,20 @@ constexpr size_t kStatusSlot = 32;  // doubles: one 256-byte slot after the scra
 
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles + kStatusSlot];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-double* g_scratch_addr[kMaxDevices] = {};  // device address of g_noalloc_scratch, per device
-
 // 256-byte alignment of every sub-array keeps warp accesses on whole segments.
 size_t round_up32(size_t n) { return (n + 31) & ~size_t(31); }
 
+// gridDim.y of the local-stage and update launches is the segment count.
+constexpr int kMaxSegments = 65535;
+
 // Device address of the scratch array on the current device.  In host code
 // `g_noalloc_scratch` names a host-side stand-in, not device memory, so the
-// address is fetched once per device, with that device current.
-int scratch_on_current_device(double** out) {
+// address is looked up with the device current.  It is looked up on every
+// call (a table lookup once the module is loaded; it allocates nothing), so a
+// context that was reset and made again never sees a stale address.  The
+// first call on a device loads the library's device code there (lazy module
+// loading), which is why that first call must come before any stream capture.
+int scratch_on_current_device(double** out, int* sms) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
@@ -50,21 +52,28 @@ int scratch_on_current_device(double** out) {
         std::snprintf(buf, sizeof buf, "solve_noncyclic_noalloc: cudaGetDevice failed: %s", cudaGetErrorString(e));
         return pbt::set_last_error(PBT_ECUDA, buf);
     }
-    if (dev < 0 || dev >= kMaxDevices) return pbt::set_last_error(PBT_EINVAL, "solve_noncyclic_noalloc: device index out of range");
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (g_scratch_addr[dev] == nullptr) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            char buf[200];
-            std::snprintf(buf, sizeof buf, "solve_noncyclic_noalloc: cudaGetSymbolAddress of the static scratch failed: %s",
-                          cudaGetErrorString(e));
-            return pbt::set_last_error(PBT_ECUDA, buf);
-        }
-        g_scratch_addr[dev] = static_cast<double*>(p);
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "solve_noncyclic_noalloc: cudaGetSymbolAddress of the static scratch failed: %s",
+                      cudaGetErrorString(e));
+        return pbt::set_last_error(PBT_ECUDA, buf);
     }
-    *out = g_scratch_addr[dev];
+    *out = static_cast<double*>(p);
+    if (cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || *sms <= 0) {
+        cudaGetLastError();
+        *sms = 1;
+    }
     return PBT_OK;
+}
+
+// Threads per block for `items` threads of work: enough CTAs to give every
+// SM two.
+int pick_threads(long long items, int sms) {
+    int tpb = 128;
+    while (tpb > 32 && (items + tpb - 1) / tpb < 2LL * sms) tpb /= 2;
+    return tpb;
 }
 
 #define PBT_NOALLOC_DISPATCH(FN)                            \
@@ -90,10 +99,11 @@ extern "C" int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, doub
         std::snprintf(buf, sizeof buf, "solve_noncyclic_noalloc: block size m=%d outside 1..%d", m, PBT_MAX_BLOCK);
         return pbt::set_last_error(PBT_EINVAL, buf);
     }
-    if (nsys <= 0 || nrow < 2 || nseg < 1 || nrow < 2 * nseg || (nseg > 1 && nrow < 3 * nseg)) {
+    if (nsys <= 0 || nrow < 2 || nseg < 1 || nseg > kMaxSegments || nrow < 2 * nseg ||
+        (nseg > 1 && nrow < 3 * nseg)) {
         std::snprintf(buf, sizeof buf,
-                      "solve_noncyclic_noalloc: needs nsys > 0, nrow >= 2, nseg >= 1 and >= 3 rows per segment "
-                      "when nseg > 1 (nsys=%d, nrow=%d, nseg=%d)", nsys, nrow, nseg);
+                      "solve_noncyclic_noalloc: needs nsys > 0, nrow >= 2, 1 <= nseg <= %d and >= 3 rows per "
+                      "segment when nseg > 1 (nsys=%d, nrow=%d, nseg=%d)", kMaxSegments, nsys, nrow, nseg);
         return pbt::set_last_error(PBT_EINVAL, buf);
     }
     if (!a || !b || !c || !d) return pbt::set_last_error(PBT_EINVAL, "solve_noncyclic_noalloc: null array pointer");
@@ -109,7 +119,8 @@ extern "C" int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, doub
         return pbt::set_last_error(PBT_EINVAL, buf);
     }
     double* base = nullptr;
-    int rc = scratch_on_current_device(&base);
+    int sms = 1;
+    int rc = scratch_on_current_device(&base, &sms);
     if (rc != PBT_OK) return rc;
 
     pbt::SolveArgs g;
@@ -128,18 +139,14 @@ extern "C" int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, doub
     g.nsys = nsys;
     g.nrow = nrow;
     g.nseg = nseg;
-    int tpb = 128;
-    while (tpb > 32 && ((long long)nsys * nseg + tpb - 1) / tpb < 2 * 152) tpb /= 2;
-    g.tpb = tpb;
+    g.tpb = pick_threads((long long)nsys * nseg, sms);
     g.stream = static_cast<cudaStream_t>(stream);
 
     cudaError_t e = cudaMemsetAsync(g.status, 0, sizeof(unsigned long long), g.stream);
     if (e == cudaSuccess) PBT_NOALLOC_DISPATCH(launch_modi)
     if (e == cudaSuccess) {
         pbt::SolveArgs g2 = g;
-        int t2 = 128;
-        while (t2 > 32 && (nsys + t2 - 1) / t2 < 2 * 152) t2 /= 2;
-        g2.tpb = t2;
+        g2.tpb = pick_threads(nsys, sms);
         {
             const pbt::SolveArgs& g = g2;
             PBT_NOALLOC_DISPATCH(launch_reduced)

@@ -35,6 +35,7 @@ struct pbt_shared {
     double* fac = nullptr;        // per row q: A_q, the factors of R_q, C'_q (3*m*m 8-byte slots, element (i,j) at
                                   // i + m*j): FP64 values, or float-float pairs (h, l) for PBT_PREC_FF
     long long* piv = nullptr;     // per row q: 4 bits per elimination step, the row swapped in
+    unsigned long long* status = nullptr;  // range failures of float-float solves (pbt_internal.h layout)
     unsigned magic = 0x50425453u;  // "PBTS"
 };
 
@@ -236,7 +237,7 @@ template <class Num, int M>
 __global__ void __launch_bounds__(kSharedThreads, (shared_min_blocks<Num, M>())) k_shared(const double* __restrict__ fac,
                                                            const long long* __restrict__ pivs,
                                                            const double* rhs, double* x, int nrow, pbt_lines L,
-                                                           int contiguous) {
+                                                           int contiguous, unsigned long long* status) {
     using T = typename Num::T;
     constexpr int K = SharedTile<M>::K, S = SharedTile<M>::S;
     __shared__ double tiles[kSharedWarps][32 * S];
@@ -260,6 +261,7 @@ __global__ void __launch_bounds__(kSharedThreads, (shared_min_blocks<Num, M>()))
     T y[M];
 #pragma unroll
     for (int i = 0; i < M; ++i) y[i] = Num::zero();
+    unsigned amax = 0;  // largest |x| written, for the range check
     for (int st = 0; st < nsteps; ++st) {
         const bool fwd = st < nchunk;
         const int q0 = (fwd ? st : 2 * nchunk - 2 - st) * K, kk = min(K, nrow - q0);
@@ -275,11 +277,14 @@ __global__ void __launch_bounds__(kSharedThreads, (shared_min_blocks<Num, M>()))
                 if (u < kk) {
                     T t[M];
 #pragma unroll
-                    for (int i = 0; i < M; ++i) t[i] = Num::in(my + u * M + i);
+                    for (int i = 0; i < M; ++i) t[i] = Num::in_rhs(my + u * M + i);
                     forward_row<Num, M>(fac, pivs, q0 + u, t, y);
                     if (last && u == kk - 1) {  // y of the last row is its solution
 #pragma unroll
-                        for (int i = 0; i < M; ++i) Num::out(my + u * M + i, y[i]);
+                        for (int i = 0; i < M; ++i) {
+                            Num::out(my + u * M + i, y[i]);
+                            amax = max(amax, Num::mag(y[i]));
+                        }
                     } else {
 #pragma unroll
                         for (int i = 0; i < M; ++i) Num::sts(my + u * M + i, y[i]);
@@ -295,7 +300,10 @@ __global__ void __launch_bounds__(kSharedThreads, (shared_min_blocks<Num, M>()))
                         for (int i = 0; i < M; ++i) t[i] = Num::lds(my + u * M + i);
                         backward_row<Num, M>(fac, q0 + u, t, y);
 #pragma unroll
-                        for (int i = 0; i < M; ++i) Num::out(my + u * M + i, y[i]);
+                        for (int i = 0; i < M; ++i) {
+                            Num::out(my + u * M + i, y[i]);
+                            amax = max(amax, Num::mag(y[i]));
+                        }
                     }
                 }
             }
@@ -307,11 +315,15 @@ __global__ void __launch_bounds__(kSharedThreads, (shared_min_blocks<Num, M>()))
                 for (int i = 0; i < M; ++i) t[i] = Num::lds(my + u * M + i);
                 backward_row<Num, M>(fac, q0 + u, t, y);
 #pragma unroll
-                for (int i = 0; i < M; ++i) Num::out(my + u * M + i, y[i]);
+                for (int i = 0; i < M; ++i) {
+                    Num::out(my + u * M + i, y[i]);
+                    amax = max(amax, Num::mag(y[i]));
+                }
             }
         }
         store<M>(x, tile, base, live, nlive, q0, kk, L, cont);
     }
+    if (live) pbt::report_status(status, pbt::range_bits<Num>(amax, true));
 }
 
 template <int M>
@@ -322,10 +334,11 @@ cudaError_t launch_shared(const pbt_shared* sh, const double* rhs, double* x, co
     if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
     const int contiguous = (L.elem_stride == 1 && L.row_stride == M) ? 1 : 0;
     if (sh->precision == PBT_PREC_FF)
-        k_shared<pbt::FF, M><<<(unsigned)grid, kSharedThreads, 0, st>>>(sh->fac, sh->piv, rhs, x, sh->nrow, L, contiguous);
+        k_shared<pbt::FF, M><<<(unsigned)grid, kSharedThreads, 0, st>>>(sh->fac, sh->piv, rhs, x, sh->nrow, L,
+                                                                        contiguous, sh->status);
     else
         k_shared<pbt::F64, M><<<(unsigned)grid, kSharedThreads, 0, st>>>(sh->fac, sh->piv, rhs, x, sh->nrow, L,
-                                                                         contiguous);
+                                                                         contiguous, sh->status);
     return cudaGetLastError();
 }
 
@@ -437,7 +450,7 @@ int pbt_shared_create(pbt_shared** out, int m, int nrow, const double* a, const 
         // (h, l) = (v rounded to float, the rest rounded to float): |l| <= ulp(h)/2.
         for (double& v : fac) {
             if (!(std::fabs(v) < 0x1p127))
-                return pbt::set_last_error(PBT_EINVAL, "shared_create: a factor is outside the float-float range");
+                return pbt::set_last_error(PBT_ERANGE, "shared_create: a factor is outside the float-float range");
             const float h = (float)v, l = (float)(v - (double)h);
             float pair[2] = {h, l};
             std::memcpy(&v, pair, sizeof v);
@@ -450,6 +463,8 @@ int pbt_shared_create(pbt_shared** out, int m, int nrow, const double* a, const 
     s->precision = precision;
     cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&s->fac), fac.size() * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&s->piv), piv.size() * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&s->status), sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(s->status, 0, sizeof(unsigned long long));
     if (e == cudaSuccess)
         e = cudaMemcpy(s->fac, fac.data(), fac.size() * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -458,6 +473,7 @@ int pbt_shared_create(pbt_shared** out, int m, int nrow, const double* a, const 
         cudaGetLastError();
         cudaFree(s->fac);
         cudaFree(s->piv);
+        cudaFree(s->status);
         delete s;
         return pbt::set_last_error(e == cudaErrorMemoryAllocation ? PBT_ENOMEM : PBT_ECUDA,
                                    (std::string("shared_create: ") + cudaGetErrorString(e)).c_str());
@@ -498,11 +514,27 @@ int pbt_shared_shape(const pbt_shared* s, int* m, int* nrow) {
     return PBT_OK;
 }
 
+int pbt_shared_status(const pbt_shared* s, void* stream) {
+    if (!s || s->magic != kSharedMagic) return pbt::set_last_error(PBT_ESTATE, "shared_status: null or destroyed handle");
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    unsigned long long w = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&w, s->status, sizeof w, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemset(s->status, 0, sizeof w);
+    if (e != cudaSuccess)
+        return pbt::set_last_error(PBT_ECUDA, (std::string("shared_status: ") + cudaGetErrorString(e)).c_str());
+    if (w & pbt::kRangeMark)
+        return pbt::set_last_error(PBT_ERANGE, "shared_status: a float-float solve left the arithmetic's range (a "
+                                               "right-hand side outside 2^-96 <= |x| < 2^96, an overflow, or a line "
+                                               "whose solution lies below 2^-100); those lines are not valid");
+    return PBT_OK;
+}
+
 int pbt_shared_destroy(pbt_shared* s) {
     if (!s) return PBT_OK;
     if (s->magic != kSharedMagic) return pbt::set_last_error(PBT_ESTATE, "shared_destroy: destroyed handle");
     cudaFree(s->fac);
     cudaFree(s->piv);
+    cudaFree(s->status);
     s->magic = 0;
     delete s;
     return PBT_OK;

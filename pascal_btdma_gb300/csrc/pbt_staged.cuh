@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const
         }
     }
 
-    bool bad = false;
+    unsigned bad = 0, amax = 0;
     T y[M];
     // This lane's C'_{q-1}: (k, j) at cps[32 * (k*M + j)]; y_{q-1}[k] at cps[32 * (M*M + k)].
     double* const cps = ring + R * M * 32 + lane;
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(32, PBT_STAGED_MIN_CTAS) k_thomas_staged(const
         {
             const double* p = take();
 PBT_UNROLL
-            for (int i = 0; i < M; ++i) xd[i] = Num::acc(Num::in(p + 32 * i));
+            for (int i = 0; i < M; ++i) xd[i] = Num::acc(Num::in_rhs(p + 32 * i));
             if constexpr (kKeepLU<Num, M>) {
                 // The refined solve's first pass keeps the right-hand side
                 // (in g.ra) as it streams by: D is solved in place.
@@ -345,7 +345,7 @@ PBT_UNROLL
             if (!last) {
                 if (active && ok) st_raw_vec<Num, M>(D + o, plane, y);
             } else {
-                if (active && ok) out_vec<Num, M>(D + o, plane, y);
+                if (active && ok) out_vec<Num, M>(D + o, plane, y, amax);
             }
         }
         const size_t plane = opaque(plane0);
@@ -430,7 +430,7 @@ PBT_UNROLL
             }
 PBT_UNROLL
             for (int i = 0; i < M; ++i) y[i] = t[i];
-            if (active && ok) out_vec<Num, M>(D + o, plane0, y);
+            if (active && ok) out_vec<Num, M>(D + o, plane0, y, amax);
             if (!ok) break;
         }
     }
@@ -454,7 +454,7 @@ PBT_UNROLL
         __syncwarp();
         return;
     }
-    if (bad && active) atomicAdd(g.status, 1ull);
+    if (active) report_status(g.status, bad | range_bits<Num>(amax, true));
 }
 
 // ---------------------------------------------------------------------------
@@ -587,7 +587,7 @@ PBT_UNROLL
         if (!ok) break;
         F32::Acc ta[M];
 PBT_UNROLL
-        for (int i = 0; i < M; ++i) ta[i] = F32::acc(FF::split(r[i]).h);
+        for (int i = 0; i < M; ++i) ta[i] = F32::acc(FF::split_wide(r[i]).h);
         if (q > 0) {
 PBT_UNROLL
             for (int k = 0; k < M; ++k)
@@ -695,14 +695,10 @@ PBT_UNROLL
             const double ed = FF::widen(e[i]);
             const double x = *px + ed;
             *px = x;
-            emax = fmax(emax, fabs(ed));
-            xmax = fmax(xmax, fabs(x));
+            refine_stat(emax, xmax, ed, x);
         }
     }
-    // NaN-safe: a non-finite or undefined ratio reports +Inf.
-    float ratio = (xmax > 0.0) ? (float)(emax / xmax) : (emax > 0.0 ? INFINITY : 0.f);
-    if (!(ratio == ratio)) ratio = INFINITY;
-    atomicMax(ra.stat, __float_as_uint(ratio));
+    refine_report(emax, xmax, ra.stat, g.status);
 }
 
 template <int M>

@@ -1,8 +1,19 @@
-// pbt_probe.cu -- FP64 / FP32 FMA rate probes (include/pbt_probe.h).
+// fma_probe.cu -- FP64 / FP32 FMA rate probes for the benchmark
+// (libpbt_probe.so, loaded by pascal_btdma_gb300/peaks.py).
+//
+// Measurement tooling, not part of the solver library or its C ABI: the
+// solve's ceilings on GB300 are the FP64 and FP32 FMA rates as well as HBM
+// bandwidth, so bench.py measures them on the device it runs on and reports
+// the kernels against them.
 #include <cuda_runtime.h>
 
-#include "../../include/pbt.h"
-#include "../../include/pbt_probe.h"
+extern "C" {
+/* Sustained fused multiply-add rates of the current device in FMA/s, from
+ * kernels with 8 independent FMA chains per thread on 4 CTAs x 256 threads
+ * per SM (best of 3 timed launches each, CUDA events).  Either pointer may be
+ * NULL.  Returns 0, or 2 when a CUDA call failed. */
+int pbt_probe_fma_rates(double* fp64_fma_per_s, double* fp32_fma_per_s);
+}
 
 namespace {
 
@@ -51,16 +62,16 @@ double rate(int sms, int iters, cudaError_t& err) {
 
 extern "C" int pbt_probe_fma_rates(double* fp64, double* fp32) {
     int dev = 0, sms = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return PBT_ECUDA;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return PBT_ECUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 2;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 2;
     cudaError_t e = cudaSuccess;
     if (fp64) {
         *fp64 = rate<double>(sms, 2048, e);
-        if (e != cudaSuccess) return PBT_ECUDA;
+        if (e != cudaSuccess) return 2;
     }
     if (fp32) {
         *fp32 = rate<float>(sms, 65536, e);
-        if (e != cudaSuccess) return PBT_ECUDA;
+        if (e != cudaSuccess) return 2;
     }
-    return PBT_OK;
+    return 0;
 }

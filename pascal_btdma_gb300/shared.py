@@ -27,6 +27,7 @@ SHARED_SIGNATURES = {
     "pbt_shared_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int, _P, _P, _P, C.c_int]),
     "pbt_shared_solve": (C.c_int, [_P, _P, _P, C.POINTER(_LinesC), _P]),
     "pbt_shared_shape": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pbt_shared_status": (C.c_int, [_P, _P]),
     "pbt_shared_destroy": (C.c_int, [_P]),
 }
 _bound = False
@@ -115,6 +116,14 @@ class SharedMatrix:
         _raise(_lib().pbt_shared_solve(self._h, C.c_void_p(rhs.data_ptr()), C.c_void_p(x.data_ptr()), C.byref(lc),
                                        C.c_void_p(s)), "SharedMatrix.solve")
         return x
+
+    def status(self, stream=None) -> None:
+        """Synchronise and raise ArithmeticRangeError if a float-float solve
+        since the last call left the arithmetic's range (pbt_shared_status)."""
+        import torch
+
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream.cuda_stream
+        _raise(_lib().pbt_shared_status(self._h, C.c_void_p(s)), "SharedMatrix.status")
 
     def destroy(self) -> None:
         if getattr(self, "_h", None):

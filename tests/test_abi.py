@@ -20,7 +20,7 @@ def declared(header: str) -> set[str]:
     return set(re.findall(r"\b(pbt_[a-z0-9_]+)\s*\(", text))
 
 
-@pytest.mark.parametrize("header,loader", [("pbt.h", N.lib), ("pbt_probe.h", N.lib), ("pbt_batch.h", N.lib),
+@pytest.mark.parametrize("header,loader", [("pbt.h", N.lib), ("pbt_batch.h", N.lib),
                                            ("pbt_shared.h", N.lib), ("pbt_synth.h", N.synth_lib)])
 def test_every_declared_symbol_is_exported(header, loader):
     lib = loader()
@@ -33,7 +33,6 @@ def test_every_declared_symbol_is_exported(header, loader):
 def test_python_signatures_cover_header():
     assert declared("pbt.h") == set(N.SIGNATURES)
     assert declared("pbt_synth.h") == set(N.SYNTH_SIGNATURES)
-    assert declared("pbt_probe.h") == set(N.PROBE_SIGNATURES)
     from pascal_btdma_gb300 import batch
 
     assert declared("pbt_batch.h") == set(batch.BATCH_SIGNATURES)
@@ -200,7 +199,7 @@ def test_shared_create_checks_before_the_gpu():
                                  N.PBT_PREC_FP32_REFINE) == N.PBT_EUNSUPPORTED
     tiny, zero = np.full(2, 1e-40), np.zeros(2)
     assert lib.pbt_shared_create(C.byref(h), 1, 2, zero.ctypes.data, tiny.ctypes.data, tiny.ctypes.data,
-                                 N.PBT_PREC_FF) == N.PBT_EINVAL
+                                 N.PBT_PREC_FF) == N.PBT_ERANGE
     assert not h.value
 
 

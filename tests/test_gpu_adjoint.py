@@ -46,7 +46,9 @@ def run_adjoint(w, nseg, prec, g):
 
 
 @pytest.mark.parametrize("m,nsys,nrow,nseg", [(1, 37, 10, 1), (2, 65, 9, 3), (3, 33, 40, 1), (4, 96, 64, 8),
-                                              (5, 70, 24, 1), (5, 64, 256, 16), (8, 9, 16, 2), (10, 5, 12, 1)])
+                                              (5, 70, 24, 1), (5, 64, 256, 16), (6, 40, 2, 1), (7, 64, 12, 1),
+                                              (7, 33, 2, 1), (8, 9, 16, 2), (8, 64, 16, 1), (9, 35, 9, 1),
+                                              (10, 5, 12, 1), (10, 64, 3, 1)])
 @pytest.mark.parametrize("prec", ["fp64", "ff"])
 def test_adjoint_matches_transposed_oracle(cuda, m, nsys, nrow, nseg, prec):
     w = synth.dominant(m, nsys, nrow, seed=300 + m, delta=1.5)
@@ -69,11 +71,13 @@ def test_adjoint_matches_transposed_oracle(cuda, m, nsys, nrow, nseg, prec):
         assert np.abs(got.reshape(m, m, nrow, nsys) - exp).max() <= 1e-13 * scale
 
 
-@pytest.mark.parametrize("nseg,prec", [(1, "fp64"), (8, "fp64"), (1, "ff"), (8, "ff")])
-def test_autograd_finite_differences(cuda, nseg, prec):
+@pytest.mark.parametrize("m,nseg,prec", [(4, 1, "fp64"), (4, 8, "fp64"), (4, 1, "ff"), (4, 8, "ff"),
+                                         (7, 1, "fp64"), (8, 1, "ff"), (9, 2, "fp64"), (10, 1, "fp64"),
+                                         (10, 1, "ff")])
+def test_autograd_finite_differences(cuda, m, nseg, prec):
     """L = sum(w * x), x = M^{-1} d; autograd gradients vs central differences
     on 64 random entries of each of A, B, C, d (h = 1e-6, FP64 solves)."""
-    m, nsys, nrow = 4, 64, 64
+    nsys, nrow = 64, 64
     wl = synth.dominant(m, nsys, nrow, seed=77, delta=1.5)
     dev = torch.device(cuda)
     A, B, C, d = (torch.from_numpy(t).to(dev).requires_grad_(True) for t in wl.arrays)

@@ -190,6 +190,26 @@ def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta):
         assert np.isfinite(D).all()
 
 
+@pytest.mark.parametrize("nseg", [2])
+def test_full_size_cyclic_against_oracle_subset(cuda, nseg):
+    """The pencil batch as periodic lines (m = 5, 65536 x 256, the bench's
+    cyclic variant) on the GPU; 48 of its systems re-solved by the oracle's
+    periodic solve (btdma_many_cycl restated)."""
+    m, nsys, nrow = 5, 65536, 256
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=2025, delta=1.2, flags=0)
+    rng = np.random.default_rng(1)
+    pick = np.unique(np.concatenate([[0, nsys - 1], rng.choice(nsys, size=46, replace=False)]))
+    ref = oracle_solve(subset(w, pick), nseg, cyclic=True)
+    for prec, tol in PREC_TOL:
+        (_, _, _, D), singular = gpu_solve(w, nseg, cyclic=True, precision=prec)
+        assert singular == 0
+        got = column_subset(m, nsys, nrow, D, pick)
+        err = per_system_relerr(m, len(pick), nrow, got, ref.D)
+        print(f"cyclic {prec} m={m} nsys={nsys} nrow={nrow} nseg={nseg}: max rel err {err:.3e}")
+        assert err <= tol
+        assert np.isfinite(D).all()
+
+
 REFINE_TOL = 1e-10  # the mixed-precision target: FP32 factorisation + FP64 residual refinement
 
 

@@ -7,7 +7,8 @@ inside a time-stepping loop).  It keeps its reduced-system scratch in a fixed
 Called here through the C ABI and compared with the plan-based entry point
 (pbt_solve_noncyclic on a plan with PBT_FLAG_INPLACE | PBT_FLAG_REFERENCE_METHOD,
 the same in-place two-stage method) on two calls in a row, at the tolerance of
-the other GPU parity tests.  This file is collected last on purpose."""
+the other GPU parity tests, and its solution directly with the oracle's.  This
+file is collected last on purpose."""
 import ctypes as C
 
 import numpy as np
@@ -17,6 +18,7 @@ import torch
 from pascal_btdma_gb300 import _native as N
 from pascal_btdma_gb300 import synth
 from conftest import per_system_relerr
+from gpu_util import oracle_solve
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -57,6 +59,7 @@ def test_noalloc_matches_plan_entry_twice(cuda):
         pa, pc, pd = planned(w, nseg, cuda)
         na, nc, nd = noalloc(w, nseg, cuda)
         assert per_system_relerr(m, nsys, nrow, nd, pd) <= TOL
+        assert per_system_relerr(m, nsys, nrow, nd, oracle_solve(w, nseg).D) <= TOL
         scale = max(np.abs(pa).max(), np.abs(pc).max())
         assert np.abs(na - pa).max() <= TOL * scale and np.abs(nc - pc).max() <= TOL * scale
 
