@@ -64,6 +64,7 @@ VARIANTS = [  # name, m, nsys, nrow, nseg, delta, cyclic
     ("pencil_P16", 5, 65536, 256, 16, 1.2, False),
     ("long_lines_P128", 4, 256, 32768, 128, 1.2, False),
     ("small_P4", 3, 1024, 128, 4, 2.0, False),  # 34.6 MB: fits in L2, timed with L2 flushed before each solve
+    ("pencil_cyclic_P1", 5, 65536, 256, 1, 1.2, True),  # periodic lines, one pass per line (k_thomas_cyclic)
     ("pencil_cyclic_P2", 5, 65536, 256, 2, 1.2, True),  # periodic lines (btdma_many_cycl), two segments
 ]
 L2_FIT_BYTES = 256 << 20  # inputs below this are timed with an L2 flush before every solve

@@ -175,7 +175,12 @@ int pbt_solve_noncyclic_profiled(pbt_plan* plan, double* a, double* b, double* c
 
 /* Replaces solve_cyclic (pascal_btdma_cuda.cu:1063-1075, which throws in the
  * reference port) and btdma_many_cycl_mpi_gpu_v2 (mod_btdma_gpu_v2.f90:200-239).
- * The plan must carry PBT_FLAG_CYCLIC and nseg >= 2. */
+ * The plan must carry PBT_FLAG_CYCLIC.  nseg >= 2 runs the two-stage method
+ * with the cyclic reduced solve (btdma_many_cycl, mod_btdma_cpu.f90:80-183);
+ * nseg = 1 (nrow >= 3) runs btdma_many_cycl's periodic block Thomas on the
+ * whole line in one launch, with the fill-in column in plan workspace
+ * (nsys * nrow * m * m doubles, also with PBT_FLAG_INPLACE, where C' goes into
+ * C and A stays untouched).  FP64 and PBT_PREC_FF. */
 int pbt_solve_cyclic(pbt_plan* plan, double* a, double* b, double* c, double* d,
                      int m, int nsys, int nrow, void* stream);
 

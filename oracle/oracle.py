@@ -31,7 +31,8 @@ def lib() -> C.CDLL:
         for name in ("pbto_solve_noncyclic", "pbto_solve_cyclic", "pbto_solve_noncyclic_cpu", "pbto_solve_cyclic_cpu"):
             getattr(_lib, name).argtypes = [I, I, I, I, P, P, P, P, I]
             getattr(_lib, name).restype = I
-        for name in ("pbto_block_thomas", "pbto_block_thomas_cpu"):
+        for name in ("pbto_block_thomas", "pbto_block_thomas_cpu", "pbto_block_thomas_cyclic",
+                     "pbto_block_thomas_cyclic_cpu"):
             getattr(_lib, name).argtypes = [I, I, I, P, P, P, P, I]
             getattr(_lib, name).restype = I
         _lib.pbto_dgesv.argtypes = [I, I, P, I, P, I]
@@ -71,6 +72,12 @@ def solve_cyclic(m, nsys, nrow, nseg, A, B, Cm, D, nthreads=0) -> int:
 
 def block_thomas(m, nsys, nrow, A, B, Cm, D, nthreads=0) -> int:
     return _check(lib().pbto_block_thomas(m, nsys, nrow, _p(A), _p(B), _p(Cm), _p(D), nthreads), "block_thomas")
+
+
+def block_thomas_cyclic(m, nsys, nrow, A, B, Cm, D, nthreads=0) -> int:
+    """A whole periodic line as one segment: btdma_many_cycl on the original rows (nrow >= 3)."""
+    return _check(lib().pbto_block_thomas_cyclic(m, nsys, nrow, _p(A), _p(B), _p(Cm), _p(D), nthreads),
+                  "block_thomas_cyclic")
 
 
 def solve_noncyclic_cpu(m, nsys, nrow, nseg, A, B, Cm, D, nthreads=0) -> int:

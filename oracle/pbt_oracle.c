@@ -5,7 +5,8 @@
  * Restates, stage by stage and in the same operation order, PaScaL_BTDMA's
  * MPI CPU path, Fortran_Original/src/mod_btdma_cpu.f90:
  *   btdma_many        :15-78    plain block Thomas (reduced solve)
- *   btdma_many_cycl   :80-183   cyclic block Thomas (cyclic reduced solve)
+ *   btdma_many_cycl   :80-183   cyclic block Thomas (cyclic reduced solve; also
+ *                               applied to a whole periodic line, one segment)
  *   btdma_many_mpi    :242-271  stage sequence, non-cyclic
  *   btdma_many_cyclic_mpi :273-302  stage sequence, cyclic
  *   btdma_many_modi   :305-443  stage 1, modified elimination of a segment
@@ -358,6 +359,7 @@ static void update(int n, int ns, int m, int s0, int s1,
 typedef struct {
     int m, nsys, N, P, cyclic, thomas;
     double *A, *B, *C, *D;
+    double* E;  /* whole-line periodic solve: the fill-in column, X(m,m,nsys,N) */
     int s0, s1;
     int bad;
     int err;
@@ -369,7 +371,13 @@ static void* run_chunk(void* arg) {
     const int s0 = jb->s0, s1 = jb->s1, cnt = s1 - s0;
     if (cnt <= 0) return NULL;
     if (jb->thomas) {
-        jb->bad += many(jb->N, ns, m, s0, s1, jb->A, jb->B, jb->C, jb->D);
+        /* One segment per line: the reference's reduced-system solvers applied
+         * to the original rows (btdma_many, or btdma_many_cycl for periodic
+         * lines, which needs N >= 3). */
+        if (jb->cyclic)
+            jb->bad += many_cycl(jb->N, ns, m, s0, s1, jb->A, jb->B, jb->C, jb->D, jb->E);
+        else
+            jb->bad += many(jb->N, ns, m, s0, s1, jb->A, jb->B, jb->C, jb->D);
         return NULL;
     }
     const int R = 2 * P;
@@ -413,15 +421,17 @@ int pbto_default_threads(void) {
 static int run_cpu_layout(int m, int nsys, int N, int P, int cyclic, int thomas,
                           double* A, double* B, double* C, double* D, int nthreads) {
     if (m < 1 || m > MAXM || nsys < 1 || P < 1 || N < 2 * P) return -1;
+    if (thomas && cyclic && N < 3) return -1;
     if (nthreads <= 0) nthreads = pbto_default_threads();
     if (nthreads > nsys) nthreads = nsys;
     chunk_job* jobs = (chunk_job*)calloc((size_t)nthreads, sizeof(chunk_job));
     pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
-    if (!jobs || !th) { free(jobs); free(th); return -2; }
+    double* E = (thomas && cyclic) ? (double*)malloc(sizeof(double) * (size_t)m * m * nsys * N) : NULL;
+    if (!jobs || !th || (thomas && cyclic && !E)) { free(jobs); free(th); free(E); return -2; }
     for (int t = 0; t < nthreads; ++t) {
         int f, l;
         pbto_partition(nsys, nthreads, t, &f, &l);
-        chunk_job j = {m, nsys, N, P, cyclic, thomas, A, B, C, D, f, l + 1, 0, 0};
+        chunk_job j = {m, nsys, N, P, cyclic, thomas, A, B, C, D, E, f, l + 1, 0, 0};
         jobs[t] = j;
     }
     for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, run_chunk, &jobs[t]);
@@ -429,7 +439,7 @@ static int run_cpu_layout(int m, int nsys, int N, int P, int cyclic, int thomas,
     for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
     int bad = 0, err = 0;
     for (int t = 0; t < nthreads; ++t) { bad += jobs[t].bad; err |= jobs[t].err; }
-    free(jobs); free(th);
+    free(jobs); free(th); free(E);
     return err ? -2 : bad;
 }
 
@@ -445,6 +455,10 @@ int pbto_solve_cyclic_cpu(int m, int nsys, int N, int P, double* A, double* B,
 int pbto_block_thomas_cpu(int m, int nsys, int N, double* A, double* B, double* C,
                           double* D, int nthreads) {
     return run_cpu_layout(m, nsys, N, 1, 0, 1, A, B, C, D, nthreads);
+}
+int pbto_block_thomas_cyclic_cpu(int m, int nsys, int N, double* A, double* B, double* C,
+                                 double* D, int nthreads) {
+    return run_cpu_layout(m, nsys, N, 1, 1, 1, A, B, C, D, nthreads);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -504,4 +518,8 @@ int pbto_solve_cyclic(int m, int nsys, int N, int P, double* A, double* B, doubl
 int pbto_block_thomas(int m, int nsys, int N, double* A, double* B, double* C, double* D,
                       int nthreads) {
     return run_gpu_layout(m, nsys, N, 1, 0, 1, A, B, C, D, nthreads);
+}
+int pbto_block_thomas_cyclic(int m, int nsys, int N, double* A, double* B, double* C, double* D,
+                             int nthreads) {
+    return run_gpu_layout(m, nsys, N, 1, 1, 1, A, B, C, D, nthreads);
 }

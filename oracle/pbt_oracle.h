@@ -66,6 +66,11 @@ int pbto_solve_cyclic(int m, int nsys, int N, int P,
 int pbto_block_thomas(int m, int nsys, int N,
                       double* A, double* B, double* C, double* D,
                       int nthreads);
+/* A whole periodic line in one segment: btdma_many_cycl
+ * (mod_btdma_cpu.f90:80-183) on the original rows, N >= 3. */
+int pbto_block_thomas_cyclic(int m, int nsys, int N,
+                             double* A, double* B, double* C, double* D,
+                             int nthreads);
 
 /* CPU-layout variants, X(m,m,nsys,N), D(m,nsys,N): what the CPU baseline times. */
 int pbto_solve_noncyclic_cpu(int m, int nsys, int N, int P, double* A, double* B,
@@ -74,6 +79,8 @@ int pbto_solve_cyclic_cpu(int m, int nsys, int N, int P, double* A, double* B,
                           double* C, double* D, int nthreads);
 int pbto_block_thomas_cpu(int m, int nsys, int N, double* A, double* B, double* C,
                           double* D, int nthreads);
+int pbto_block_thomas_cyclic_cpu(int m, int nsys, int N, double* A, double* B, double* C,
+                                 double* D, int nthreads);
 
 /* Layout transposes between the GPU layout and the CPU layout. */
 void pbto_gpu_to_cpu(int m, int nsys, int N, int is_matrix, const double* g, double* c);

@@ -295,7 +295,8 @@ def solve_noncyclic_profiled(plan, a, b, c, d, m, nsys, nrow, timings=None, stre
 
 def solve_cyclic(plan, a, b, c, d, m, nsys, nrow, stream=None) -> None:
     """Periodic lines (mod_btdma_gpu_v2.f90:200-239); needs a plan created with
-    ``cyclic=True`` and ``nseg >= 2``."""
+    ``cyclic=True``; ``nseg = 1`` (``nrow >= 3``) solves each periodic line in
+    one pass, ``nseg >= 2`` by the two-stage method."""
     _solve(N.lib().pbt_solve_cyclic, "solve_cyclic", plan, a, b, c, d, m, nsys, nrow, stream)
 
 

@@ -47,12 +47,13 @@ struct pbt_plan {
     int device = 0;
     int sms = 0;          // multiprocessors of `device`
     bool thomas = false;  // single-segment plain block Thomas path
+    bool cyclic_thomas = false;  // single-segment periodic block Thomas (k_thomas_cyclic)
     double* aw = nullptr;  // factor workspace (nullptr when in place)
     double* cw = nullptr;
     double* ra = nullptr;
     double* rc = nullptr;
     double* rd = nullptr;
-    double* re = nullptr;
+    double* re = nullptr;  // cyclic fill-in column: reduced rows, or every row (cyclic_thomas)
     unsigned long long* status = nullptr;
     // Iterative refinement (PBT_PREC_FP32_REFINE): iterate X, correction /
     // residual E, convergence statistic, and the outcome of the last solve.
@@ -199,6 +200,7 @@ cudaError_t run_refine_staged(int m, const pbt::SolveArgs& g, const pbt::ThomasM
 }
 
 PBT_DISPATCH(run_thomas, launch_thomas)
+PBT_DISPATCH(run_thomas_cyclic, launch_thomas_cyclic)
 
 cudaError_t run_thomas_lines(int arith, int m, const pbt::SolveArgs& g, const pbt::LineStrides& ls) {
     if (arith == kFF) {
@@ -381,8 +383,15 @@ int validate(const pbt_plan_desc& d) {
                       3 * d.nseg);
         return fail(PBT_EINVAL, buf);
     }
-    if ((d.flags & PBT_FLAG_CYCLIC) && d.nseg < 2) {
-        return fail(PBT_EINVAL, "plan: the cyclic solve needs nseg >= 2 (a reduced system of at least 4 rows)");
+    if ((d.flags & PBT_FLAG_CYCLIC) && d.nseg == 1) {
+        // One segment: the whole-line periodic block Thomas.  The reference
+        // method (modified elimination + cyclic reduced solve) needs a reduced
+        // system of at least 4 rows, i.e. nseg >= 2.
+        if (d.flags & PBT_FLAG_REFERENCE_METHOD)
+            return fail(PBT_EINVAL, "plan: the reference method of the cyclic solve needs nseg >= 2 (a reduced "
+                                    "system of at least 4 rows)");
+        if (d.nrow < 3)
+            return fail(PBT_EINVAL, "plan: a periodic line needs nrow >= 3");
     }
     if (d.precision != PBT_PREC_FP64 && d.precision != PBT_PREC_FF && d.precision != PBT_PREC_FP32_REFINE) {
         return fail(PBT_EUNSUPPORTED, "plan: unknown precision");
@@ -653,8 +662,10 @@ int solve_core(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
         if (rc) return rc;
         for (int i = 1; i < 5; ++i)
             if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
-    } else if (p->thomas) {
-        e = thomas_launch(p, arith_of(ds.precision), m, make_args(p, a, b, c, d, s, nsys));
+    } else if (p->thomas || p->cyclic_thomas) {
+        const pbt::SolveArgs g = make_args(p, a, b, c, d, s, nsys);
+        e = p->thomas ? thomas_launch(p, arith_of(ds.precision), m, g)
+                      : run_thomas_cyclic(arith_of(ds.precision), m, g);
         if (e != cudaSuccess) return cuda_fail(e, "block Thomas launch");
         for (int i = 1; i < 5; ++i)
             if ((e = mark(i)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
@@ -700,7 +711,7 @@ int solve_core(pbt_plan* p, double* a, double* b, double* c, double* d, int m, i
         for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], evs.ev[i], evs.ev[i + 1]);
         float tot = 0;
         cudaEventElapsedTime(&tot, evs.ev[0], evs.ev[4]);
-        if (p->thomas) {
+        if (p->thomas || p->cyclic_thomas) {
             // One fused launch: all of it is local compute.
             t->local_compute = tot * 1e-3;
             t->forward_exchange = t->reduced_compute = t->backward_exchange = t->update_compute = 0.0;
@@ -748,6 +759,7 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
     const bool inplace = (d.flags & PBT_FLAG_INPLACE) != 0;
     const bool cyclic = (d.flags & PBT_FLAG_CYCLIC) != 0;
     p->thomas = (d.nseg == 1) && !cyclic && !(d.flags & PBT_FLAG_REFERENCE_METHOD);
+    p->cyclic_thomas = (d.nseg == 1) && cyclic;
     const size_t mm = (size_t)d.m * d.m;
     const size_t rows = (size_t)d.nsys * d.nrow;
     const size_t rrows = (size_t)d.nsys * 2 * d.nseg;
@@ -758,10 +770,13 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
         // systems, m*m + 1 runs of 32 floats.
         const bool keep_lu = p->thomas && d.precision == PBT_PREC_FP32_REFINE && d.m <= pbt::kStagedMaxBlock;
         const size_t lu_doubles = (size_t)d.nrow * ((d.nsys + 31) / 32) * 16 * (mm + 1);
-        if (!p->thomas && (rc = alloc(p, &p->aw, mm * rows))) goto fail_out;
+        if (!p->thomas && !p->cyclic_thomas && (rc = alloc(p, &p->aw, mm * rows))) goto fail_out;
         if (keep_lu && (rc = alloc(p, &p->aw, lu_doubles))) goto fail_out;
     }
-    if (!p->thomas) {
+    if (p->cyclic_thomas) {
+        // The fill-in column of every row (also with PBT_FLAG_INPLACE).
+        if ((rc = alloc(p, &p->re, mm * rows))) goto fail_out;
+    } else if (!p->thomas) {
         if ((rc = alloc(p, &p->ra, mm * rrows))) goto fail_out;
         if ((rc = alloc(p, &p->rc, mm * rrows))) goto fail_out;
         if ((rc = alloc(p, &p->rd, (size_t)d.m * rrows))) goto fail_out;

@@ -18,6 +18,7 @@
 namespace pbt {
 template cudaError_t launch_thomas<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_thomas_lines<PBT_NUM, PBT_M>(const SolveArgs&, const LineStrides&);
+template cudaError_t launch_thomas_cyclic<PBT_NUM, PBT_M>(const SolveArgs&);
 #if PBT_M <= 6
 template cudaError_t launch_thomas_staged<PBT_NUM, PBT_M>(const SolveArgs&, const ThomasMaps&);
 #endif

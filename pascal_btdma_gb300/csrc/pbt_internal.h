@@ -75,6 +75,9 @@ template <class Num, int M> cudaError_t launch_thomas_lines(const SolveArgs& g, 
 cudaError_t launch_lines_layout(const double* src, double* dst, const LineStrides& ls, int E, int nsys, int nrow,
                                 int dir, cudaStream_t s);
 template <class Num, int M> cudaError_t launch_thomas_staged(const SolveArgs& g, const ThomasMaps& maps);
+// Periodic lines in one segment (k_thomas_cyclic): the fill-in column in
+// g.re, nsys * nrow * m * m raw values; nrow >= 3.
+template <class Num, int M> cudaError_t launch_thomas_cyclic(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_modi(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced(const SolveArgs& g);
 template <class Num, int M> cudaError_t launch_reduced_cyclic(const SolveArgs& g);

@@ -157,11 +157,14 @@ PBT_UNROLL
 // ---------------------------------------------------------------------------
 template <class Num, int M>
 struct LU {
-    static_assert(M <= 8, "LU::piv packs the M - 1 pivot rows in 4 bits each");
+    static_assert(M <= 16, "LU::piv packs the M - 1 pivot rows in 4 bits each");
+    // Pivot rows of blocks up to 8 x 8 fit 32 bits (the staged kernels store
+    // them as one float); larger blocks take 64.
+    using Piv = typename std::conditional<(M <= 8), unsigned, unsigned long long>::type;
     // f[k][c] (c > k): row k of U, normalised; f[i][k] (i > k): multiplier
     // l_ik of step k; f[k][k]: 1 / U_kk.
     typename Num::T f[M][M];
-    unsigned piv = 0;    // 4 bits per step k: the row swapped with row k
+    Piv piv = 0;         // 4 bits per step k: the row swapped with row k
     unsigned swaps = 0;  // bit k: some thread of the warp swapped at step k
 };
 
@@ -194,7 +197,7 @@ PBT_UNROLL
                     }
                 }
             }
-            lu.piv |= static_cast<unsigned>(p) << (4 * k);
+            lu.piv |= static_cast<typename LU<Num, M>::Piv>(p) << (4 * k);
         }
         const T pv = Num::fin(a[k][k]);
         bad |= Num::is_zero(pv);
@@ -224,7 +227,7 @@ __device__ __forceinline__ void lu_solve(const LU<Num, M>& lu, typename Num::Acc
 PBT_UNROLL
     for (int k = 0; k < M; ++k) {
         if (k + 1 < M && ((lu.swaps >> k) & 1u)) {
-            const unsigned p = (lu.piv >> (4 * k)) & 15u;
+            const unsigned p = static_cast<unsigned>((lu.piv >> (4 * k)) & 15u);
 PBT_UNROLL
             for (int i = k + 1; i < M; ++i) {
                 const unsigned s = (p == static_cast<unsigned>(i));
@@ -691,6 +694,302 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_lines(const SolveArgs g
         thomas_body<Num, M>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, (size_t)ls.elem, (size_t)ls.row, g.nrow,
                             g.factors_raw != 0, bad);
     }
+    report_status(g.status, bad);
+}
+
+// ---------------------------------------------------------------------------
+// Periodic lines in one segment: btdma_many_cycl
+// (Fortran_Original/src/mod_btdma_cpu.f90:80-183) applied to the whole line,
+// the GPU counterpart of the two-stage cyclic solve with P = 1.  Row 0 is the
+// anchor; rows 1..N-1 are eliminated with the fill-in column e, which carries
+// the coupling to x_0 (e_1 = -A_1, e_{N-1} = -C_{N-1}, zero in between):
+//   forward, q = 1..N-1:  R_q = B_q - A_q C'_{q-1} (R_1 = B_1),
+//     [y_q | e'_q | C'_q] = R_q^{-1} [d_q - A_q y_{q-1} | e_q - A_q e'_{q-1} | C_q]
+//   backward, q = N-2..1: y_q -= C'_q y_{q+1},  e'_q -= C'_q e'_{q+1}
+//   row 0: (B_0 + A_0 e'_{N-1} + C_0 e'_1) x_0 = d_0 - A_0 y_{N-1} - C_0 y_1
+//   rows 1..N-1: x_q = y_q + e'_q x_0.
+// The row step is split as in thomas_body_lu: R_q is factored once and y, the
+// m columns of e' and the m columns of C' are solved one column at a time.
+// Per thread, shared memory holds C'_{q-1} (slots k*M + j), y_{q-1} (M*M + k)
+// and e'_{q-1} (kE + k*M + j).  Before the factorisation, W = A_q e'_{q-1}
+// replaces e'_{q-1} in its slots (the product the reference forms with
+// dgemm), so that no m x m accumulator block beyond R is live at a time; the
+// e-columns then overwrite W column by column.  e' goes to EW (raw values of
+// the arithmetic, nsys * N * m * m), C' to CW as in k_thomas, y (then the
+// back-substituted y) to D.  Needs N >= 3.
+// ---------------------------------------------------------------------------
+template <class Num, int M>
+__host__ __device__ constexpr int cyclic_slots() {
+    return 2 * M * M + M;
+}
+
+template <class Num, int M>
+__device__ __forceinline__ void thomas_cyclic_body(const double* A, const double* B, const double* C, double* D,
+                                                   double* CW, double* EW, double* cps, int cstride, size_t plane0,
+                                                   size_t rs, int N, bool raw, unsigned& bad) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    constexpr int kY = M * M;      // y_{q-1}
+    constexpr int kE = M * M + M;  // e'_{q-1}, then W, then e'_q
+    // Column loops rolled for float-float (code size, as in thomas_body_lu)
+    // and from m = 5 on in FP64 too: unrolled, the FP64 m = 5 body spills
+    // ~0.6 KB a thread at the 128-register cap, rolled it spills nothing.
+    constexpr bool kRolled = lu_rolled<Num>() || M >= 5;
+    auto slot = [&](int s) -> double* { return cps + s * cstride; };
+    T y[M];
+    for (int q = 1; q < N; ++q) {
+        const size_t o = (size_t)q * rs;
+        const bool last = (q == N - 1);
+        // W = A_q e'_{q-1} into the e slots; row 1: W = A_1 (its e is -A_1).
+        if (q == 1) {
+            const size_t plane = opaque(plane0);
+            const double* pa = A + o;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) Num::sts(slot(kE + i * M + j), Num::in(pa));
+        } else {
+            const size_t plane = opaque(plane0);
+            const double* pa = A + o;
+            Acc w[M][M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) w[i][j] = Num::acc0();
+#pragma unroll(kRolled ? 1 : M)
+            for (int k = 0; k < M; ++k) {
+                T ak[M], ek[M];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) ak[i] = Num::in(pa);
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ek[j] = Num::lds(slot(kE + k * M + j));
+PBT_UNROLL
+                for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::mac(w[i][j], ak[i], ek[j]);
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) Num::sts(slot(kE + i * M + j), Num::fin(w[i][j]));
+        }
+        Acc r[M][M], xd[M];
+        {
+            const size_t plane = opaque(plane0);
+            const double* pd = D + o;
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pd += plane) xd[i] = Num::acc(Num::in_rhs(pd));
+        }
+        {
+            const size_t plane = opaque(plane0);
+            const double* pb = B + o;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pb += plane) r[i][j] = Num::acc(Num::in_ro(pb));
+        }
+        if (q > 1) {
+            const size_t plane = opaque(plane0);
+            const double* pa = A + o;
+#pragma unroll(kRolled ? 1 : M)
+            for (int k = 0; k < M; ++k) {
+                T ck[M];
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ck[j] = Num::lds(slot(k * M + j));
+                T yk;
+                if constexpr (kRolled)
+                    yk = Num::lds(slot(kY + k));
+                else
+                    yk = y[k];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) {
+                    const T a = Num::in(pa);
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
+                    Num::msub(xd[i], a, yk);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+        LU<Num, M> lu;
+        lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, xd, y);
+        if constexpr (kRolled) {
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
+        }
+        st_raw_vec<Num, M>(D + o, opaque(plane0), y);
+        // The e-columns: e_q - W, e_q = -C_{N-1} on the last row, else 0.
+        {
+            const size_t plane = opaque(plane0);
+            double* pe = EW + o;
+            const double* pc = C + o;
+#pragma unroll(kRolled ? 1 : M)
+            for (int j = 0; j < M; ++j) {
+                Acc v[M];
+                T xj[M];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pc += plane) {
+                    const T w = Num::lds(slot(kE + i * M + j));
+                    if (last) {
+                        v[i] = Num::acc(Num::neg(Num::in(pc)));
+                        Num::msub(v[i], w, Num::one());
+                    } else {
+                        v[i] = Num::acc(Num::neg(w));
+                    }
+                }
+                lu_solve<Num, M>(lu, v, xj);
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pe += plane) {
+                    Num::sts(pe, xj[i]);
+                    Num::sts(slot(kE + i * M + j), xj[i]);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+        if (last) break;
+        {
+            const size_t plane = opaque(plane0);
+            const double* pc = C + o;
+            double* pw = CW + o;
+#pragma unroll(kRolled ? 1 : M)
+            for (int j = 0; j < M; ++j) {
+                Acc cj[M];
+                T xj[M];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pc += plane) cj[i] = Num::acc(Num::in(pc));
+                lu_solve<Num, M>(lu, cj, xj);
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pw += plane) {
+                    if (raw || !Num::kConv)
+                        Num::sts(pw, xj[i]);
+                    else
+                        Num::out(pw, xj[i]);
+                    Num::sts(slot(i * M + j), xj[i]);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+    }
+    // Row 0 needs e'_{N-1} and y_{N-1} as the forward sweep left them: they
+    // move to the C' and y slots, which the backward sweep does not use.
+PBT_UNROLL
+    for (int s = 0; s < M * M; ++s) Num::sts(slot(s), Num::lds(slot(kE + s)));
+PBT_UNROLL
+    for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
+    for (int q = N - 2; q >= 1; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T c[M][M], t[M];
+        ld_fac_blk<Num, M>(c, CW + o, plane, raw);
+        ld_raw_vec<Num, M>(t, D + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+            t[i] = Num::fin(s);
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) y[i] = t[i];
+        st_raw_vec<Num, M>(D + o, plane, y);
+        double* pe = EW + o;
+#pragma unroll(kRolled ? 1 : M)
+        for (int j = 0; j < M; ++j) {
+            T ej[M], nv[M];
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) ej[k] = Num::lds(slot(kE + k * M + j));
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                Acc s = Num::acc(Num::lds(pe + (size_t)i * plane));
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], ej[k]);
+                nv[i] = Num::fin(s);
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pe += plane) {
+                Num::sts(pe, nv[i]);
+                Num::sts(slot(kE + i * M + j), nv[i]);
+            }
+        }
+    }
+    // Row 0; y = y_1 and the e slots hold e'_1 (both back-substituted).
+    // R_0 and its right-hand side are accumulated by outer products, one
+    // column of A_0 (then of C_0) at a time, so that only R_0 and one column
+    // are live; each entry still sums its terms in the order B, A_0 e'_{N-1}
+    // (k ascending), C_0 e'_1 (k ascending).
+    unsigned amax = 0;
+    T x0[M];
+    {
+        Acc r[M][M], t[M];
+        {
+            const size_t plane = opaque(plane0);
+            const double* pd = D;
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pd += plane) t[i] = Num::acc(Num::in_rhs(pd));
+            const double* pb = B;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pb += plane) r[i][j] = Num::acc(Num::in_ro(pb));
+        }
+PBT_UNROLL
+        for (int h = 0; h < 2; ++h) {
+            // h = 0: A_0 with e'_{N-1}, y_{N-1} (C' and y slots); h = 1: C_0
+            // with e'_1 (e slots) and y_1 (registers).
+            const size_t plane = opaque(plane0);
+            const double* pa = (h == 0 ? A : C);
+            const int es = (h == 0 ? 0 : kE);
+#pragma unroll(kRolled ? 1 : M)
+            for (int k = 0; k < M; ++k) {
+                T ak[M], ek[M];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) ak[i] = Num::in(pa);
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ek[j] = Num::lds(slot(es + k * M + j));
+                const T yk = (h == 0) ? Num::lds(slot(kY + k)) : y[k];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::mac(r[i][j], ak[i], ek[j]);
+                    Num::msub(t[i], ak[i], yk);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+        LU<Num, M> lu;
+        lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, t, x0);
+        out_vec<Num, M>(D, opaque(plane0), x0, amax);
+    }
+    for (int q = 1; q < N; ++q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T e[M][M], t[M];
+        ld_raw_blk<Num, M>(e, EW + o, plane);
+        ld_raw_vec<Num, M>(t, D + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::mac(s, e[i][k], x0[k]);
+            t[i] = Num::fin(s);
+        }
+        out_vec<Num, M>(D + o, plane, t, amax);
+    }
+    bad |= range_bits<Num>(amax, true);
+}
+
+template <class Num, int M>
+__global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_cyclic(const SolveArgs g) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    extern __shared__ double thomas_cps[];
+    unsigned bad = 0;
+    thomas_cyclic_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, g.re + sys,
+                               thomas_cps + threadIdx.x, blockDim.x, (size_t)g.nsys * g.nrow, (size_t)g.nsys,
+                               g.nrow, g.factors_raw != 0, bad);
     report_status(g.status, bad);
 }
 
@@ -1662,6 +1961,25 @@ cudaError_t launch_thomas_lines(const SolveArgs& g, const LineStrides& ls) {
         const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
         const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * (M * M + M) * sizeof(double) : 0;
         k_thomas_lines<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g, ls);
+        return cudaGetLastError();
+    }
+}
+// Block sizes above 6 run 32-thread CTAs (their slots take 0.9-1.7 KB a
+// thread); above 48 KB a CTA the kernel opts in to the larger carve-out.
+template <class Num, int M>
+cudaError_t launch_thomas_cyclic(const SolveArgs& g) {
+    if constexpr (std::is_same<Num, F32>::value) {
+        return cudaErrorInvalidValue;  // FP64 and float-float plans only
+    } else {
+        int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
+        if (M > 6) tpb = 32;
+        const size_t smem = (size_t)tpb * cyclic_slots<Num, M>() * sizeof(double);
+        if (smem > 48u * 1024u) {
+            const cudaError_t e = cudaFuncSetAttribute(k_thomas_cyclic<Num, M>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        k_thomas_cyclic<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g);
         return cudaGetLastError();
     }
 }

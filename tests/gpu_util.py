@@ -23,7 +23,12 @@ def gpu_solve(w, nseg=1, dev="cuda:0", cyclic=False, stream=None, **plan_kw):
 
 
 def oracle_solve(w, nseg=1, cyclic=False):
+    """The oracle on a copy of ``w``: the two-stage method, or for periodic
+    lines in one segment, btdma_many_cycl on the whole line."""
     r = w.copy()
+    if cyclic and nseg == 1:
+        O.block_thomas_cyclic(w.m, w.nsys, w.nrow, *r.arrays)
+        return r
     fn = O.solve_cyclic if cyclic else O.solve_noncyclic
     fn(w.m, w.nsys, w.nrow, nseg, *r.arrays)
     return r

@@ -103,7 +103,8 @@ def create(**kw):
         (dict(nseg=0), N.PBT_EINVAL, "nseg"),
         (dict(nrow=8, nseg=3), N.PBT_EINVAL, "nseg"),
         (dict(nrow=10, nseg=4), N.PBT_EINVAL, ">= 3 rows"),
-        (dict(flags=N.PBT_FLAG_CYCLIC), N.PBT_EINVAL, "cyclic"),
+        (dict(flags=N.PBT_FLAG_CYCLIC, nrow=2), N.PBT_EINVAL, "nrow >= 3"),
+        (dict(flags=N.PBT_FLAG_CYCLIC | N.PBT_FLAG_REFERENCE_METHOD), N.PBT_EINVAL, "nseg >= 2"),
         (dict(flags=0x100), N.PBT_EINVAL, "unknown flag"),
         (dict(flags=N.PBT_FLAG_DIRECT_LOADS | N.PBT_FLAG_STAGED_LOADS), N.PBT_EINVAL, "exclude each other"),
         (dict(flags=N.PBT_FLAG_CPU_LAYOUT | N.PBT_FLAG_INPLACE), N.PBT_EUNSUPPORTED, "CPU_LAYOUT"),

@@ -75,6 +75,52 @@ def test_cyclic_matches_oracle(cuda, m, nsys, nrow, nseg, prec, tol):
     assert per_system_relerr(m, nsys, nrow, D, ref.D) <= tol
 
 
+CYCLIC_P1 = [  # m, nsys, nrow: periodic lines in one segment, m = 1..10, ragged warps, nrow down to 3
+    (1, 33, 3), (1, 37, 10), (2, 65, 4), (2, 40, 16), (3, 70, 12), (3, 129, 5), (4, 64, 24), (4, 31, 40),
+    (5, 31, 30), (5, 96, 64), (6, 17, 18), (7, 9, 9), (8, 20, 16), (9, 11, 12), (10, 7, 30),
+]
+
+
+@pytest.mark.parametrize("m,nsys,nrow", CYCLIC_P1)
+@pytest.mark.parametrize("delta", [1.05, 1.5])
+@pytest.mark.parametrize("prec,tol", PREC_TOL)
+def test_cyclic_single_segment_matches_oracle(cuda, m, nsys, nrow, delta, prec, tol):
+    """k_thomas_cyclic against btdma_many_cycl applied to the whole line."""
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=17 * m + nrow, delta=delta, flags=0)
+    (A, B, C, D), singular = gpu_solve(w, 1, cyclic=True, precision=prec)
+    assert singular == 0
+    ref = oracle_solve(w, 1, cyclic=True)
+    assert per_system_relerr(m, nsys, nrow, D, ref.D) <= tol
+    # A, B and C are left untouched by a workspace plan.
+    assert np.array_equal(A, w.A) and np.array_equal(B, w.B) and np.array_equal(C, w.C)
+
+
+@pytest.mark.parametrize("m,nsys,nrow", [(2, 65, 9), (5, 70, 24), (8, 9, 12)])
+@pytest.mark.parametrize("prec,tol", PREC_TOL)
+def test_cyclic_single_segment_inplace_and_two_stage(cuda, m, nsys, nrow, prec, tol):
+    """In place (C' into C, A untouched) it gives the workspace plan's x, and
+    the single-segment solve agrees with the two-stage cyclic method."""
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=31 + m, delta=1.3, flags=0)
+    (_, _, _, D1), _ = gpu_solve(w, 1, cyclic=True, precision=prec)
+    (A2, _, C2, D2), _ = gpu_solve(w, 1, cyclic=True, precision=prec, inplace=True)
+    (_, _, _, D3), _ = gpu_solve(w, 2, cyclic=True, precision=prec)
+    assert per_system_relerr(m, nsys, nrow, D2, D1) <= tol
+    assert per_system_relerr(m, nsys, nrow, D3, D1) <= tol
+    assert np.array_equal(A2, w.A) and not np.array_equal(C2, w.C)
+
+
+def test_cyclic_single_segment_singular_block_reported(cuda):
+    """A zero diagonal block on a periodic line is counted, as in the other solves."""
+    m, nsys, nrow = 3, 40, 8
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=4, delta=1.5, flags=0)
+    B = w.B.reshape(m * m, nrow, nsys)
+    B[:, 3, 5] = 0.0
+    A = w.A.reshape(m * m, nrow, nsys)
+    A[:, 3, 5] = 0.0
+    (_, _, _, _), singular = gpu_solve(w, 1, cyclic=True)
+    assert singular >= 1
+
+
 def test_manufactured_solution(cuda):
     w = synth.manufactured(3, 256, 64, seed=2)
     (_, _, _, D), _ = gpu_solve(w, 4)
@@ -190,7 +236,7 @@ def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta):
         assert np.isfinite(D).all()
 
 
-@pytest.mark.parametrize("nseg", [2])
+@pytest.mark.parametrize("nseg", [1, 2])
 def test_full_size_cyclic_against_oracle_subset(cuda, nseg):
     """The pencil batch as periodic lines (m = 5, 65536 x 256, the bench's
     cyclic variant) on the GPU; 48 of its systems re-solved by the oracle's

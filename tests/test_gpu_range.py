@@ -127,12 +127,13 @@ def test_tiny_solution_is_reported(cuda):
 def test_cyclic_and_adjoint_report(cuda):
     w = synth.fill(synth.DOMINANT, 3, 50, 24, seed=3, delta=1.5, flags=0)
     w.C[7] = 2.0 ** 100
-    a, b, c, d = to_dev(w.arrays, cuda)
-    with pbt.BtdmaGpuPlan() as plan:
-        plan.create(3, 50, 24, 2, cyclic=True, precision="ff")
-        pbt.solve_cyclic(plan, a, b, c, d, 3, 50, 24)
-        with pytest.raises(pbt.ArithmeticRangeError):
-            plan.status()
+    for nseg in (1, 2):
+        a, b, c, d = to_dev(w.arrays, cuda)
+        with pbt.BtdmaGpuPlan() as plan:
+            plan.create(3, 50, 24, nseg, cyclic=True, precision="ff")
+            pbt.solve_cyclic(plan, a, b, c, d, 3, 50, 24)
+            with pytest.raises(pbt.ArithmeticRangeError):
+                plan.status()
     w = synth.dominant(3, 50, 24, seed=4, delta=1.5)
     a, b, c, d = to_dev(w.arrays, cuda)
     g = torch.ones_like(d)

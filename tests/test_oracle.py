@@ -89,6 +89,30 @@ def test_cyclic_matches_dense_solve(m, nsys, nrow, nseg):
         assert np.abs(xo - x).max() <= 1e-12 * np.abs(x).max()
 
 
+@pytest.mark.parametrize("m,nsys,nrow", [(1, 3, 3), (1, 5, 8), (2, 3, 4), (3, 4, 12), (4, 2, 24), (5, 3, 30),
+                                         (6, 2, 7), (8, 2, 12), (10, 2, 9)])
+def test_whole_line_cyclic_matches_dense_solve(m, nsys, nrow):
+    """btdma_many_cycl applied to a whole periodic line (one segment)."""
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=11 + m, delta=1.5, flags=0)
+    got = w.copy()
+    assert O.block_thomas_cyclic(m, nsys, nrow, *got.arrays) == 0
+    for s in range(nsys):
+        M, rhs = O.assemble_dense(m, nsys, nrow, *w.arrays, s, cyclic=True)
+        x = np.linalg.solve(M, rhs)
+        xo = O.solution_of(m, nsys, nrow, got.D, s)
+        assert np.abs(xo - x).max() <= 1e-12 * np.abs(x).max()
+    # The CPU-layout entry gives the same bits.
+    c = [O.gpu_to_cpu(m, nsys, nrow, i < 3, v) for i, v in enumerate(w.arrays)]
+    assert O.lib().pbto_block_thomas_cyclic_cpu(m, nsys, nrow, *[O._p(v) for v in c], 0) == 0
+    assert np.array_equal(O.cpu_to_gpu(m, nsys, nrow, False, c[3]), got.D)
+
+
+def test_whole_line_cyclic_needs_three_rows():
+    w = synth.fill(synth.DOMINANT, 2, 2, 2, seed=1, delta=1.5, flags=0)
+    with pytest.raises(ValueError):
+        O.block_thomas_cyclic(2, 2, 2, *w.copy().arrays)
+
+
 def test_matches_banded_lapack():
     m, nsys, nrow, nseg = 3, 4, 128, 4  # the small config, 4 systems
     w = synth.dominant(m, nsys, nrow, seed=1, delta=2.0)
