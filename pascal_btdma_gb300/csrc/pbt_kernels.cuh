@@ -718,6 +718,25 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_lines(const SolveArgs g
 // the arithmetic, nsys * N * m * m), C' to CW as in k_thomas, y (then the
 // back-substituted y) to D.  Needs N >= 3.
 // ---------------------------------------------------------------------------
+// Column k of a block (M raw FP64 values, `plane` apart, read through `pa`,
+// which advances by one column per call) into `cur`: with Ahead, `nxt`
+// already holds column k and column k + 1 is loaded into it.
+template <int M, bool Ahead>
+__device__ __forceinline__ void ld_col_ahead(double (&cur)[M], double (&nxt)[M], const double*& pa, size_t plane,
+                                             int k) {
+    if constexpr (Ahead) {
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) cur[i] = nxt[i];
+        if (k + 1 < M) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pa += plane) nxt[i] = __ldg(pa);
+        }
+    } else {
+PBT_UNROLL
+        for (int i = 0; i < M; ++i, pa += plane) cur[i] = __ldg(pa);
+    }
+}
+
 template <class Num, int M>
 __host__ __device__ constexpr int cyclic_slots() {
     return 2 * M * M + M;
@@ -735,6 +754,8 @@ __device__ __forceinline__ void thomas_cyclic_body(const double* A, const double
     // and from m = 5 on in FP64 too: unrolled, the FP64 m = 5 body spills
     // ~0.6 KB a thread at the 128-register cap, rolled it spills nothing.
     constexpr bool kRolled = lu_rolled<Num>() || M >= 5;
+    // A's columns one ahead up to m = 5 (at m = 6 the extra registers spill).
+    constexpr bool kPrefetchA = M <= 5;
     auto slot = [&](int s) -> double* { return cps + s * cstride; };
     T y[M];
     for (int q = 1; q < N; ++q) {
@@ -756,11 +777,20 @@ PBT_UNROLL
             for (int i = 0; i < M; ++i)
 PBT_UNROLL
                 for (int j = 0; j < M; ++j) w[i][j] = Num::acc0();
+            // kPrefetchA: column k + 1 of A is loaded (raw) before column k
+            // is used.
+            double an[M];
+            if constexpr (kPrefetchA) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) an[i] = __ldg(pa);
+            }
 #pragma unroll(kRolled ? 1 : M)
             for (int k = 0; k < M; ++k) {
                 T ak[M], ek[M];
+                double ac[M];
+                ld_col_ahead<M, kPrefetchA>(ac, an, pa, plane, k);
 PBT_UNROLL
-                for (int i = 0; i < M; ++i, pa += plane) ak[i] = Num::in(pa);
+                for (int i = 0; i < M; ++i) ak[i] = Num::in(&ac[i]);
 PBT_UNROLL
                 for (int j = 0; j < M; ++j) ek[j] = Num::lds(slot(kE + k * M + j));
 PBT_UNROLL
@@ -792,6 +822,11 @@ PBT_UNROLL
         if (q > 1) {
             const size_t plane = opaque(plane0);
             const double* pa = A + o;
+            double an[M];
+            if constexpr (kPrefetchA) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) an[i] = __ldg(pa);
+            }
 #pragma unroll(kRolled ? 1 : M)
             for (int k = 0; k < M; ++k) {
                 T ck[M];
@@ -802,9 +837,11 @@ PBT_UNROLL
                     yk = Num::lds(slot(kY + k));
                 else
                     yk = y[k];
+                double ac[M];
+                ld_col_ahead<M, kPrefetchA>(ac, an, pa, plane, k);
 PBT_UNROLL
-                for (int i = 0; i < M; ++i, pa += plane) {
-                    const T a = Num::in(pa);
+                for (int i = 0; i < M; ++i) {
+                    const T a = Num::in(&ac[i]);
 PBT_UNROLL
                     for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
                     Num::msub(xd[i], a, yk);
@@ -820,57 +857,50 @@ PBT_UNROLL
             for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
         }
         st_raw_vec<Num, M>(D + o, opaque(plane0), y);
-        // The e-columns: e_q - W, e_q = -C_{N-1} on the last row, else 0.
+        // The 2m right-hand-side columns in one rolled loop (one copy of the
+        // column solve's code): jj < m, column jj of e_q - W (e_q = -C_{N-1}
+        // on the last row, else 0) into EW and the e slots; jj >= m, column
+        // jj - m of C_q into CW and the C' slots (not on the last row).
         {
             const size_t plane = opaque(plane0);
-            double* pe = EW + o;
-            const double* pc = C + o;
-#pragma unroll(kRolled ? 1 : M)
-            for (int j = 0; j < M; ++j) {
+            const int ncol = last ? M : 2 * M;
+#pragma unroll 1
+            for (int jj = 0; jj < ncol; ++jj) {
+                const bool ecol = jj < M;
+                const int j = ecol ? jj : jj - M;
+                const double* pc = C + o + (size_t)(M * j) * plane;
                 Acc v[M];
                 T xj[M];
+                if (ecol) {
 PBT_UNROLL
-                for (int i = 0; i < M; ++i, pc += plane) {
-                    const T w = Num::lds(slot(kE + i * M + j));
-                    if (last) {
-                        v[i] = Num::acc(Num::neg(Num::in(pc)));
-                        Num::msub(v[i], w, Num::one());
-                    } else {
-                        v[i] = Num::acc(Num::neg(w));
+                    for (int i = 0; i < M; ++i) {
+                        const T w = Num::lds(slot(kE + i * M + j));
+                        if (last) {
+                            v[i] = Num::acc(Num::neg(Num::in(pc + (size_t)i * plane)));
+                            Num::msub(v[i], w, Num::one());
+                        } else {
+                            v[i] = Num::acc(Num::neg(w));
+                        }
                     }
+                } else {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) v[i] = Num::acc(Num::in(pc + (size_t)i * plane));
                 }
                 lu_solve<Num, M>(lu, v, xj);
+                double* pw = (ecol ? EW : CW) + o + (size_t)(M * j) * plane;
+                const int s0 = ecol ? kE + j : j;
 PBT_UNROLL
-                for (int i = 0; i < M; ++i, pe += plane) {
-                    Num::sts(pe, xj[i]);
-                    Num::sts(slot(kE + i * M + j), xj[i]);
+                for (int i = 0; i < M; ++i) {
+                    if (ecol || raw || !Num::kConv)
+                        Num::sts(pw + (size_t)i * plane, xj[i]);
+                    else
+                        Num::out(pw + (size_t)i * plane, xj[i]);
+                    Num::sts(slot(s0 + i * M), xj[i]);
                 }
                 if (PBT_ROW_FENCE) mem_fence_compiler();
             }
         }
         if (last) break;
-        {
-            const size_t plane = opaque(plane0);
-            const double* pc = C + o;
-            double* pw = CW + o;
-#pragma unroll(kRolled ? 1 : M)
-            for (int j = 0; j < M; ++j) {
-                Acc cj[M];
-                T xj[M];
-PBT_UNROLL
-                for (int i = 0; i < M; ++i, pc += plane) cj[i] = Num::acc(Num::in(pc));
-                lu_solve<Num, M>(lu, cj, xj);
-PBT_UNROLL
-                for (int i = 0; i < M; ++i, pw += plane) {
-                    if (raw || !Num::kConv)
-                        Num::sts(pw, xj[i]);
-                    else
-                        Num::out(pw, xj[i]);
-                    Num::sts(slot(i * M + j), xj[i]);
-                }
-                if (PBT_ROW_FENCE) mem_fence_compiler();
-            }
-        }
     }
     // Row 0 needs e'_{N-1} and y_{N-1} as the forward sweep left them: they
     // move to the C' and y slots, which the backward sweep does not use.
@@ -895,14 +925,32 @@ PBT_UNROLL
         for (int i = 0; i < M; ++i) y[i] = t[i];
         st_raw_vec<Num, M>(D + o, plane, y);
         double* pe = EW + o;
+        // e'_q's columns one ahead (raw 8-byte values).
+        double en[M], ec[M];
+        const double* pn = pe;
+        if constexpr (kPrefetchA) {
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pn += plane) en[i] = *pn;
+        }
 #pragma unroll(kRolled ? 1 : M)
         for (int j = 0; j < M; ++j) {
             T ej[M], nv[M];
 PBT_UNROLL
             for (int k = 0; k < M; ++k) ej[k] = Num::lds(slot(kE + k * M + j));
+            if constexpr (kPrefetchA) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) ec[i] = en[i];
+                if (j + 1 < M) {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i, pn += plane) en[i] = *pn;
+                }
+            } else {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pn += plane) ec[i] = *pn;
+            }
 PBT_UNROLL
             for (int i = 0; i < M; ++i) {
-                Acc s = Num::acc(Num::lds(pe + (size_t)i * plane));
+                Acc s = Num::acc(Num::from_raw(ec[i]));
 PBT_UNROLL
                 for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], ej[k]);
                 nv[i] = Num::fin(s);

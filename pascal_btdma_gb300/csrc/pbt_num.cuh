@@ -17,7 +17,8 @@
 //   in(p)        load an FP64 matrix element (A, B, C) and convert to T
 //   in_rhs(p)    the same for a right-hand-side element (D)
 //   out(p, v)    convert T to FP64 and store (f64(v): the converted value)
-//   lds/sts      raw 8-byte workspace slots (no conversion)
+//   lds/sts      raw 8-byte workspace slots (no conversion); from_raw: a slot's
+//                8 bytes already in a register
 //   acc(x), mac(acc, x, y) (acc += x*y), msub(acc, x, y) (acc -= x*y), fin(acc)
 //   mul, rcp, neg, zero, one, key (|x| as an ordered integer), sel, is_zero
 //   nonfinite(v), mag(v), kTinyMag: the solution range check (no-ops for F64)
@@ -68,6 +69,8 @@ struct F64 {
     __device__ static __forceinline__ double f64(T v) { return v; }
     __device__ static __forceinline__ T lds(const double* p) { return *p; }
     __device__ static __forceinline__ void sts(double* p, T v) { *p = v; }
+    // A raw 8-byte slot already loaded into a register.
+    __device__ static __forceinline__ T from_raw(double v) { return v; }
 
     __device__ static __forceinline__ Acc acc(T x) { return {x}; }
     __device__ static __forceinline__ Acc acc0() { return {0.0}; }
@@ -199,6 +202,9 @@ struct FF {
         return {f.x, f.y};
     }
     __device__ static __forceinline__ void sts(double* p, T v) { *reinterpret_cast<float2*>(p) = make_float2(v.h, v.l); }
+    __device__ static __forceinline__ T from_raw(double v) {
+        return {__int_as_float(__double2loint(v)), __int_as_float(__double2hiint(v))};
+    }
 
     __device__ static __forceinline__ Acc acc(T x) { return {x.h, x.l}; }
     __device__ static __forceinline__ Acc acc0() { return {0.f, 0.f}; }
@@ -268,6 +274,7 @@ struct F32 {
     // sector of a warp's store is complete and L2 never has to fetch the rest.
     __device__ static __forceinline__ T lds(const double* p) { return reinterpret_cast<const float2*>(p)->x; }
     __device__ static __forceinline__ void sts(double* p, T v) { *reinterpret_cast<float2*>(p) = make_float2(v, 0.f); }
+    __device__ static __forceinline__ T from_raw(double v) { return __int_as_float(__double2loint(v)); }
 
     __device__ static __forceinline__ Acc acc(T x) { return {x}; }
     __device__ static __forceinline__ Acc acc0() { return {0.f}; }
