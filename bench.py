@@ -638,8 +638,14 @@ def run_ours(args):
         entry = {"m": vm, "nsys": vns, "nrow": vn, "nseg": vp, "cyclic": vcyc,
                  "l2": "flushed before each solve" if vrows * bytes_per_row(vm) < L2_FIT_BYTES else "inputs > L2"}
         xs = {}
-        for prec in ("ff", "fp64"):
-            vplan = pbt.BtdmaGpuPlan().create(vm, vns, vn, vp, precision=prec, cyclic=vcyc)
+        # With nseg > 1 a batch that fills the GPU is solved one segment per
+        # line; "<prec>_segmented" keeps the nseg segments (the two-stage
+        # method, PBT_FLAG_REFERENCE_METHOD).
+        modes = [(p_, False) for p_ in ("ff", "fp64")] + ([(p_, True) for p_ in ("ff", "fp64")] if vp > 1 else [])
+        for prec, segmented in modes:
+            key = prec + ("_segmented" if segmented else "")
+            vplan = pbt.BtdmaGpuPlan().create(vm, vns, vn, vp, precision=prec, cyclic=vcyc,
+                                              reference_method=segmented)
             ksteps = max(3, args.steps // 2)
             small = vrows * bytes_per_row(vm) < L2_FIT_BYTES
             if small:
@@ -647,13 +653,13 @@ def run_ours(args):
             else:
                 vs = time_device(vplan, (va, vb, vc), [vd], vm, vns, vn, ksteps, 3, ws, dev, vsolve)
             vs = max_over_ranks(vs, ws, dev)
-            xs[prec] = vd.clone()
+            xs[key] = vd.clone()
             if vcyc:
-                vsolve(vplan, va, vb, vc, xs[prec], vm, vns, vn)
+                vsolve(vplan, va, vb, vc, xs[key], vm, vns, vn)
                 t = None
             else:
-                t = pbt.solve_noncyclic_profiled(vplan, va, vb, vc, xs[prec], vm, vns, vn)
-            entry[prec] = {
+                t = pbt.solve_noncyclic_profiled(vplan, va, vb, vc, xs[key], vm, vns, vn)
+            entry[key] = {
                 "block_rows_per_s": ws * vrows * ksteps / vs,
                 "ms_per_step": vs / ksteps * 1e3,
                 "algorithmic_gbs": vrows * bytes_per_row(vm) / (vs / ksteps) / 1e9,
@@ -663,6 +669,8 @@ def run_ours(args):
             }
             vplan.destroy()
         entry["ff_rel_err_vs_fp64"] = rel_err_vs(xs["ff"], xs["fp64"], vm, vns, vn)
+        if vp > 1:
+            entry["ff_segmented_rel_err_vs_fp64"] = rel_err_vs(xs["ff_segmented"], xs["fp64"], vm, vns, vn)
         variants[name] = entry
         del va, vb, vc, vd, vw, xs
         torch.cuda.empty_cache()
@@ -681,19 +689,24 @@ def run_ours(args):
             with pbt.BtdmaGpuPlan() as p64:
                 p64.create(M, NSYS, NROW, nseg_m, precision="fp64")
                 solve(p64, ma, mb, mc, ref, M, NSYS, NROW)
-            for prec in ("fp32_refine", "ff"):
+            modes = [(p_, False) for p_ in ("fp32_refine", "ff")]
+            if nseg_m > 1:
+                modes += [(p_, True) for p_ in ("fp32_refine", "ff", "fp64")]
+            for prec, segmented in modes:
+                key = prec + ("_segmented" if segmented else "")
                 with pbt.BtdmaGpuPlan() as pl:
-                    pl.create(M, NSYS, NROW, nseg_m, precision=prec, tol=1e-12, max_iter=8)
+                    pl.create(M, NSYS, NROW, nseg_m, precision=prec, tol=1e-12, max_iter=8,
+                              reference_method=segmented)
                     ms = time_device(pl, (ma, mb, mc), [md], M, NSYS, NROW, 3, 3, ws, dev, solve)
                     ms = max_over_ranks(ms, ws, dev)
                     xo = md.clone()
                     solve(pl, ma, mb, mc, xo, M, NSYS, NROW)
                     info = pl.refine_info() if prec == "fp32_refine" else (None, None)
-                entry[prec] = {"block_rows_per_s": ws * mrows * 3 / ms, "ms_per_step": ms / 3 * 1e3,
-                               "rel_err_vs_fp64": rel_err_vs(xo, ref, M, NSYS, NROW)}
+                entry[key] = {"block_rows_per_s": ws * mrows * 3 / ms, "ms_per_step": ms / 3 * 1e3,
+                              "rel_err_vs_fp64": rel_err_vs(xo, ref, M, NSYS, NROW)}
                 if prec == "fp32_refine":
-                    entry[prec]["fp32_solves"] = info[0]
-                    entry[prec]["last_correction"] = info[1]
+                    entry[key]["fp32_solves"] = info[0]
+                    entry[key]["last_correction"] = info[1]
                 del xo
             mixed[f"delta{delta}_P{nseg_m}"] = entry
             del ref

@@ -107,7 +107,7 @@ typedef enum pbt_precision {
 /* Plan flags. */
 #define PBT_FLAG_CYCLIC 0x1u           /* periodic lines: plan for pbt_solve_cyclic */
 #define PBT_FLAG_INPLACE 0x2u          /* A, C receive the elimination factors; no factor workspace */
-#define PBT_FLAG_REFERENCE_METHOD 0x4u /* always run the two-stage (modified Thomas) method, even at nseg = 1 */
+#define PBT_FLAG_REFERENCE_METHOD 0x4u /* always run the two-stage (modified Thomas) method on the nseg segments, even at nseg = 1 or for a batch that fills the GPU */
 #define PBT_FLAG_DIRECT_LOADS 0x8u     /* single-segment solve: always direct global loads */
 #define PBT_FLAG_STAGED_LOADS 0x10u    /* single-segment solve: TMA-staged loads wherever allowed (m <= 6,
                                           nsys >= 32 and even, 16-byte aligned arrays) */
@@ -150,7 +150,13 @@ void pbt_plan_desc_init(pbt_plan_desc* desc);
 /* Replaces BtdmaGpuPlan::create(m, nsys, nrow, comm) (pascal_btdma_cuda.cu:956-1005)
  * and btdma_makeplan_gpu_v2 (mod_btdma_gpu_v2.f90:70-109): validates the
  * sizes and allocates the device workspace on the current device.
- * Non-cyclic, FP64. */
+ * Non-cyclic, FP64.
+ * nseg stands for the reference's MPI ranks.  A batch large enough to fill
+ * the GPU with one thread per system (nsys >= 128 * SMs, 19456 on a GB300)
+ * is solved one segment per line whatever nseg says: the single-segment
+ * method does ~40 % of the two-stage method's arithmetic and gives the same x
+ * to rounding.  PBT_FLAG_REFERENCE_METHOD keeps the nseg segments (and the
+ * reference's in-place A', C' with PBT_FLAG_INPLACE). */
 int pbt_plan_create(pbt_plan** plan, int m, int nsys, int nrow, int nseg);
 
 /* As pbt_plan_create with every option of pbt_plan_desc. */
@@ -209,8 +215,9 @@ typedef struct pbt_lines {
  * euler3d_mpi_gpu.f90:931-1017) around btdma_many_mpi_gpu_v2: with
  * U(n1,n2,n3,m) and trA(n1,n2,n3,m,m) the y sweep is
  *   {n1, n3, 1, n1*n2, n1, n1*n2*n3}.
- * The plan must be a single-segment, non-cyclic FP64 or PBT_PREC_FF plan
- * (nseg = 1, no PBT_FLAG_REFERENCE_METHOD / PBT_FLAG_CPU_LAYOUT) with
+ * The plan must be a non-cyclic FP64 or PBT_PREC_FF plan solved one
+ * segment per line (nseg = 1, or a batch that fills the GPU; no
+ * PBT_FLAG_REFERENCE_METHOD / PBT_FLAG_CPU_LAYOUT) with
  * nsys = nsys_inner * nsys_outer; otherwise PBT_EUNSUPPORTED / PBT_EINVAL.
  * A PBT_FLAG_INPLACE plan writes C' into C, as the reference does; any other
  * plan keeps its factors in its workspace, addressed with the same strides,

@@ -355,6 +355,16 @@ PBT_DISPATCH(run_reduced, launch_reduced)
 PBT_DISPATCH(run_reduced_cyclic, launch_reduced_cyclic)
 PBT_DISPATCH(run_update, launch_update)
 
+// Whether a batch fills the GPU with one thread per system: at least 4 warps
+// per SM.  Measured on GB300: the m = 5 pencil batch (65536 systems, 13.5
+// warps per SM) solves in 6.2 ms as one segment per line against 18.7 ms in 16
+// segments (float-float); m = 4, 16384 systems (3.4 warps per SM): 4.55 ms in
+// one segment, 4.51 ms in 8.
+bool fills_gpu(int nsys, int sms) {
+    const long long warps = (nsys + 31) / 32;
+    return warps >= 4LL * (sms > 0 ? sms : 152);
+}
+
 // The local-stage and update launches put the segments in gridDim.y.
 constexpr int kMaxSegments = 65535;
 
@@ -758,8 +768,15 @@ int pbt_plan_create_ex(pbt_plan** out, const pbt_plan_desc* desc) {
     const auto& d = *desc;
     const bool inplace = (d.flags & PBT_FLAG_INPLACE) != 0;
     const bool cyclic = (d.flags & PBT_FLAG_CYCLIC) != 0;
-    p->thomas = (d.nseg == 1) && !cyclic && !(d.flags & PBT_FLAG_REFERENCE_METHOD);
-    p->cyclic_thomas = (d.nseg == 1) && cyclic;
+    // nseg is the reference's decomposition of a line over MPI ranks.  On one
+    // GPU, a batch with enough systems to fill it is solved one segment per
+    // line (the method of nseg = 1: ~40 % of the two-stage method's
+    // arithmetic, same x to rounding) unless PBT_FLAG_REFERENCE_METHOD asks for
+    // the segments.
+    const bool one_seg = d.nseg == 1 || (!(d.flags & PBT_FLAG_REFERENCE_METHOD) && fills_gpu(d.nsys, p->sms) &&
+                                         (!cyclic || d.nrow >= 3));
+    p->thomas = one_seg && !cyclic && !(d.flags & PBT_FLAG_REFERENCE_METHOD);
+    p->cyclic_thomas = one_seg && cyclic;
     const size_t mm = (size_t)d.m * d.m;
     const size_t rows = (size_t)d.nsys * d.nrow;
     const size_t rrows = (size_t)d.nsys * 2 * d.nseg;

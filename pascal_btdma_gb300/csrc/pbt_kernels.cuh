@@ -315,12 +315,31 @@ PBT_UNROLL
             for (int i = 0; i < M; ++i) Num::out(base + (size_t)(i + M * j) * plane, x[i][j]);
     }
 }
+// One factor value.  In place, factors are FP64 values of the library's own
+// intermediates, so they convert without the input window (Num::in_rhs): A'
+// decays along a segment, C' = R^{-1} C can be far smaller than C, and
+// neither is out of the solve's range when it falls below 2^-96.
+template <class Num>
+__device__ __forceinline__ typename Num::T ld_fac(const double* p, bool raw) {
+    return (raw || !Num::kConv) ? Num::lds(p) : Num::in_rhs(p);
+}
+template <class Num>
+__device__ __forceinline__ void st_fac(double* p, typename Num::T v, bool raw) {
+    if (raw || !Num::kConv)
+        Num::sts(p, v);
+    else
+        Num::out(p, v);
+}
 template <class Num, int M>
 __device__ __forceinline__ void ld_fac_blk(typename Num::T (&x)[M][M], const double* base, size_t plane, bool raw) {
-    if (raw || !Num::kConv)
+    if (raw || !Num::kConv) {
         ld_raw_blk<Num, M>(x, base, plane);
-    else
-        in_blk<Num, M>(x, base, plane);
+    } else {
+PBT_UNROLL
+        for (int j = 0; j < M; ++j)
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) x[i][j] = Num::in_rhs(base + (size_t)(i + M * j) * plane);
+    }
 }
 
 template <class Num, int M>
@@ -1173,13 +1192,8 @@ PBT_UNROLL
 PBT_UNROLL
         for (int i = 0; i < M; ++i) {
             T c0[M];
-            if (raw || !Num::kConv) {
 PBT_UNROLL
-                for (int k = 0; k < M; ++k) c0[k] = Num::lds(CW + (size_t)(i + M * k) * plane);
-            } else {
-PBT_UNROLL
-                for (int k = 0; k < M; ++k) c0[k] = Num::in(CW + (size_t)(i + M * k) * plane);
-            }
+            for (int k = 0; k < M; ++k) c0[k] = ld_fac<Num>(CW + (size_t)(i + M * k) * plane, raw);
             Acc t = Num::acc(Num::lds(D + (size_t)i * plane));
 PBT_UNROLL
             for (int k = 0; k < M; ++k) Num::msub(t, c0[k], dp[k]);
@@ -1202,8 +1216,7 @@ PBT_UNROLL
         for (int i = 0; i < M; ++i)
 PBT_UNROLL
             for (int j = 0; j < M; ++j) {
-                const double* p = AW + (size_t)(i + M * j) * plane;
-                x[i][j] = Num::acc((raw || !Num::kConv) ? Num::lds(p) : Num::in(p));
+                x[i][j] = Num::acc(ld_fac<Num>(AW + (size_t)(i + M * j) * plane, raw));
             }
         gesv<Num, M, 2 * M + 1>(r, x, bad);
 PBT_UNROLL
@@ -1223,6 +1236,326 @@ PBT_UNROLL
         st_raw_blk<Num, M>(RC + ro, rplane, cp);
         st_raw_vec<Num, M>(RD + ro, rplane, dp);
     }
+}
+
+#ifndef PBT_MODI_LU_MIN
+#define PBT_MODI_LU_MIN 5
+#endif
+// The local stage with the row step split (lu_factor / lu_solve), for the
+// register-resident block sizes where the fused 2m+1-column elimination of
+// modi_body spills (m = 5: ~1.5 KB a thread at 255 registers, 8 warps an SM).
+// Same algebra and storage as modi_body, organised like thomas_cyclic_body:
+// per thread, shared memory holds C'_{q-1} (slots k*M + j), d'_{q-1} (M*M + k)
+// and A'_{q-1} (kE + k*M + j); W = A_q A'_{q-1} (the reference's dgemm)
+// replaces A'_{q-1} in its slots before R_q is formed, so at most one m x m
+// accumulator block is live; R_q is factored once and d', the m columns of A'
+// and the m columns of C' are solved one column at a time (one rolled loop).
+// The backward sweep and the first row's step work column by column the same
+// way, with the carried row's A' and C' in the slots.  64-thread CTAs at 128
+// registers: 16 warps an SM where the shared memory allows.
+// Not for FP32 (the refined solve's corrections): its single-float values fit
+// the fused form's 255 registers with few spills, and the split form measured
+// slower there (pencil batch, P = 16, two FP32 solves per refined solve:
+// 23.4 ms against 18.2 ms).
+template <class Num, int M>
+__host__ __device__ constexpr bool modi_uses_lu() {
+    return M >= PBT_MODI_LU_MIN && M <= 6 && !std::is_same<Num, F32>::value;
+}
+
+template <class Num, int M>
+__device__ __forceinline__ void modi_body_lu(const double* A, const double* B, const double* C, double* D,
+                                             double* AW, double* CW, double* cps, int cstride, size_t plane0,
+                                             size_t rs, int n, bool raw, double* RA, double* RC, double* RD,
+                                             size_t rplane, size_t rrs, int seg, unsigned& bad) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    constexpr int kY = M * M;      // d'_{q-1}
+    constexpr int kE = M * M + M;  // A'_{q-1}, then W, then A'_q
+    constexpr bool kPrefetchA = M <= 5;
+    auto slot = [&](int s) -> double* { return cps + s * cstride; };
+    T y[M];  // d' of the row just solved (the carried row in the backward sweep)
+
+    // Forward.  Rows 0, 1: [A'|C'|d'] = B^{-1}[A|C|d]; rows 2..n-1:
+    // R = B - A C'_{q-1}; [A'|C'|d'] = R^{-1}[-A A'_{q-1} | C | d - A d'_{q-1}].
+    for (int q = 0; q < n; ++q) {
+        const size_t o = (size_t)q * rs;
+        const bool first2 = (q < 2);
+        if (!first2) {
+            const size_t plane = opaque(plane0);
+            const double* pa = A + o;
+            Acc w[M][M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) w[i][j] = Num::acc0();
+            double an[M];
+            if constexpr (kPrefetchA) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) an[i] = __ldg(pa);
+            }
+#pragma unroll 1
+            for (int k = 0; k < M; ++k) {
+                T ak[M], ek[M];
+                double ac[M];
+                ld_col_ahead<M, kPrefetchA>(ac, an, pa, plane, k);
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) ak[i] = Num::in(&ac[i]);
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ek[j] = Num::lds(slot(kE + k * M + j));
+PBT_UNROLL
+                for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::mac(w[i][j], ak[i], ek[j]);
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) Num::sts(slot(kE + i * M + j), Num::fin(w[i][j]));
+        }
+        Acc r[M][M], xd[M];
+        {
+            const size_t plane = opaque(plane0);
+            const double* pd = D + o;
+PBT_UNROLL
+            for (int i = 0; i < M; ++i, pd += plane) xd[i] = Num::acc(Num::in_rhs(pd));
+            const double* pb = B + o;
+PBT_UNROLL
+            for (int j = 0; j < M; ++j)
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pb += plane) r[i][j] = Num::acc(Num::in_ro(pb));
+        }
+        if (!first2) {
+            const size_t plane = opaque(plane0);
+            const double* pa = A + o;
+            double an[M];
+            if constexpr (kPrefetchA) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) an[i] = __ldg(pa);
+            }
+#pragma unroll 1
+            for (int k = 0; k < M; ++k) {
+                T ck[M];
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ck[j] = Num::lds(slot(k * M + j));
+                const T yk = Num::lds(slot(kY + k));
+                double ac[M];
+                ld_col_ahead<M, kPrefetchA>(ac, an, pa, plane, k);
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) {
+                    const T a = Num::in(&ac[i]);
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::msub(r[i][j], a, ck[j]);
+                    Num::msub(xd[i], a, yk);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+        LU<Num, M> lu;
+        lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, xd, y);
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
+        st_raw_vec<Num, M>(D + o, opaque(plane0), y);
+        // jj < m: column jj of A' (right-hand side A on rows 0, 1, else -W);
+        // jj >= m: column jj - m of C'.
+        {
+            const size_t plane = opaque(plane0);
+#pragma unroll 1
+            for (int jj = 0; jj < 2 * M; ++jj) {
+                const bool acol = jj < M;
+                const int j = acol ? jj : jj - M;
+                const size_t co = o + (size_t)(M * j) * plane;
+                Acc v[M];
+                T xj[M];
+                if (acol && !first2) {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) v[i] = Num::acc(Num::neg(Num::lds(slot(kE + i * M + j))));
+                } else {
+                    const double* ps = (acol ? A : C) + co;
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) v[i] = Num::acc(Num::in(ps + (size_t)i * plane));
+                }
+                lu_solve<Num, M>(lu, v, xj);
+                double* pw = (acol ? AW : CW) + co;
+                const int s0 = acol ? kE + j : j;
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) {
+                    st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
+                    Num::sts(slot(s0 + i * M), xj[i]);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+    }
+    // Reduced row 2*seg+1 = the segment's last row (A'_n, C'_n, d'_n).
+    {
+        const size_t ro = rrs * (size_t)(2 * seg + 1);
+PBT_UNROLL
+        for (int j = 0; j < M; ++j)
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                Num::sts(RA + ro + (size_t)(i + M * j) * rplane, Num::lds(slot(kE + i * M + j)));
+                Num::sts(RC + ro + (size_t)(i + M * j) * rplane, Num::lds(slot(i * M + j)));
+            }
+        st_raw_vec<Num, M>(RD + ro, rplane, y);
+    }
+    // Backward, rows n-3 .. 1 (0-based), carried row q+1 starting at n-2:
+    // A'_q -= C'_q A'_{q+1};  C'_q = -C'_q C'_{q+1};  d'_q -= C'_q d'_{q+1}.
+    if (n >= 3) {
+        const int q1 = (n >= 4) ? n - 2 : 1;
+        const size_t o1 = (size_t)q1 * rs;
+        const size_t plane = opaque(plane0);
+PBT_UNROLL
+        for (int j = 0; j < M; ++j)
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                const size_t e = (size_t)(i + M * j) * plane;
+                Num::sts(slot(kE + i * M + j), ld_fac<Num>(AW + o1 + e, raw));
+                Num::sts(slot(i * M + j), ld_fac<Num>(CW + o1 + e, raw));
+            }
+        ld_raw_vec<Num, M>(y, D + o1, plane);
+    }
+    for (int q = n - 3; q >= 1; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T c[M][M], t[M];
+        ld_fac_blk<Num, M>(c, CW + o, plane, raw);
+        ld_raw_vec<Num, M>(t, D + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+            t[i] = Num::fin(s);
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) y[i] = t[i];
+        st_raw_vec<Num, M>(D + o, plane, y);
+#pragma unroll 1
+        for (int jj = 0; jj < 2 * M; ++jj) {
+            const bool acol = jj < M;
+            const int j = acol ? jj : jj - M;
+            const int s0 = acol ? kE + j : j;
+            double* pw = (acol ? AW : CW) + o + (size_t)(M * j) * plane;
+            T cj[M], nv[M];
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) cj[k] = Num::lds(slot(s0 + k * M));
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                Acc s = acol ? Num::acc(ld_fac<Num>(pw + (size_t)i * plane, raw)) : Num::acc0();
+PBT_UNROLL
+                for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], cj[k]);
+                nv[i] = Num::fin(s);
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                st_fac<Num>(pw + (size_t)i * plane, nv[i], raw);
+                Num::sts(slot(s0 + i * M), nv[i]);
+            }
+            if (PBT_ROW_FENCE) mem_fence_compiler();
+        }
+    }
+    // Row 0: R = I - C'_0 A'_1;
+    // [A'_0 | C'_0 | d'_0] = R^{-1} [A'_0 | -C'_0 C'_1 | d'_0 - C'_0 d'_1],
+    // with row 1's values (A'_1, C'_1 in the slots, d'_1 in y, which moves to
+    // its slots for the rolled loop below).  W2 = C'_0 C'_1 replaces C'_1 in
+    // its slots first.
+    {
+        const size_t plane = opaque(plane0);
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
+        {
+            Acc w[M][M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) w[i][j] = Num::acc0();
+#pragma unroll 1
+            for (int k = 0; k < M; ++k) {
+                T ck[M], ek[M];
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) ck[i] = ld_fac<Num>(CW + (size_t)(i + M * k) * plane, raw);
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ek[j] = Num::lds(slot(k * M + j));
+PBT_UNROLL
+                for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::mac(w[i][j], ck[i], ek[j]);
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) Num::sts(slot(i * M + j), Num::fin(w[i][j]));
+        }
+        Acc r[M][M], xd[M];
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            xd[i] = Num::acc(Num::lds(D + (size_t)i * plane));
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) r[i][j] = Num::acc(i == j ? Num::one() : Num::zero());
+        }
+#pragma unroll 1
+        for (int k = 0; k < M; ++k) {
+            T ck[M], ek[M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) ck[i] = ld_fac<Num>(CW + (size_t)(i + M * k) * plane, raw);
+PBT_UNROLL
+            for (int j = 0; j < M; ++j) ek[j] = Num::lds(slot(kE + k * M + j));
+            const T yk = Num::lds(slot(kY + k));
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) Num::msub(r[i][j], ck[i], ek[j]);
+                Num::msub(xd[i], ck[i], yk);
+            }
+            if (PBT_ROW_FENCE) mem_fence_compiler();
+        }
+        LU<Num, M> lu;
+        lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, xd, y);
+        st_raw_vec<Num, M>(D, plane, y);
+        const size_t ro = rrs * (size_t)(2 * seg);
+        st_raw_vec<Num, M>(RD + ro, rplane, y);
+#pragma unroll 1
+        for (int jj = 0; jj < 2 * M; ++jj) {
+            const bool acol = jj < M;
+            const int j = acol ? jj : jj - M;
+            double* pw = (acol ? AW : CW) + (size_t)(M * j) * plane;
+            Acc v[M];
+            T xj[M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i)
+                v[i] = acol ? Num::acc(ld_fac<Num>(pw + (size_t)i * plane, raw))
+                            : Num::acc(Num::neg(Num::lds(slot(j + i * M))));
+            lu_solve<Num, M>(lu, v, xj);
+            double* pr = (acol ? RA : RC) + ro + (size_t)(M * j) * rplane;
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
+                Num::sts(pr + (size_t)i * rplane, xj[i]);
+            }
+            if (PBT_ROW_FENCE) mem_fence_compiler();
+        }
+    }
+}
+
+template <class Num, int M>
+__global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_modi_lu(const SolveArgs g) {
+    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sys >= g.nsys) return;
+    extern __shared__ double thomas_cps[];
+    const int seg = blockIdx.y;
+    int f, l;
+    seg_rows(g.nrow, g.nseg, seg, f, l);
+    const size_t rs = (size_t)g.nsys;
+    const size_t fo = (size_t)f * rs + sys;
+    unsigned bad = 0;
+    modi_body_lu<Num, M>(g.a + fo, g.b + fo, g.c + fo, g.d + fo, g.aw + fo, g.cw + fo, thomas_cps + threadIdx.x,
+                         blockDim.x, rs * g.nrow, rs, l - f + 1, g.factors_raw != 0, g.ra + sys, g.rc + sys,
+                         g.rd + sys, rs * 2 * g.nseg, rs, seg, bad);
+    report_status(g.status, bad);
 }
 
 template <class Num, int M>
@@ -2033,8 +2366,15 @@ cudaError_t launch_thomas_cyclic(const SolveArgs& g) {
 }
 template <class Num, int M>
 cudaError_t launch_modi(const SolveArgs& g) {
-    dim3 grid(grid_x(g.nsys, g.tpb), (unsigned)g.nseg);
-    k_modi<Num, M><<<grid, g.tpb, 0, g.stream>>>(g);
+    if constexpr (modi_uses_lu<Num, M>()) {
+        const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
+        const size_t smem = (size_t)tpb * cyclic_slots<Num, M>() * sizeof(double);
+        dim3 grid(grid_x(g.nsys, tpb), (unsigned)g.nseg);
+        k_modi_lu<Num, M><<<grid, tpb, smem, g.stream>>>(g);
+    } else {
+        dim3 grid(grid_x(g.nsys, g.tpb), (unsigned)g.nseg);
+        k_modi<Num, M><<<grid, g.tpb, 0, g.stream>>>(g);
+    }
     return cudaGetLastError();
 }
 template <class Num, int M>

@@ -184,6 +184,27 @@ def test_profiled_timings(cuda):
             assert t.reduced_compute > 0 and t.update_compute > 0
 
 
+@pytest.mark.parametrize("cyclic", [False, True])
+def test_batch_filling_the_gpu_runs_one_segment(cuda, cyclic):
+    """A plan whose batch fills the GPU (at least 4 warps of systems per SM:
+    19456 systems on 152 SMs; here 32768) solves one segment per line whatever
+    nseg says: the same bits as an nseg = 1 plan, and the oracle's segmented x
+    to rounding; PBT_FLAG_REFERENCE_METHOD keeps the segments."""
+    m, nsys, nrow, nseg = 3, 32768, 24, 4
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=8, delta=1.5, flags=0 if cyclic else synth.ZERO_ENDS)
+    for prec, tol in PREC_TOL:
+        (_, _, _, D4), _ = gpu_solve(w, nseg, cyclic=cyclic, precision=prec)
+        (_, _, _, D1), _ = gpu_solve(w, 1, cyclic=cyclic, precision=prec)
+        (_, _, _, Dr), _ = gpu_solve(w, nseg, cyclic=cyclic, precision=prec, reference_method=True)
+        assert np.array_equal(D4, D1)
+        assert not np.array_equal(Dr, D1)
+        sub = subset(w, np.arange(0, nsys, 1024))
+        ref = oracle_solve(sub, nseg, cyclic=cyclic)
+        for D in (D4, Dr):
+            got = column_subset(m, nsys, nrow, D, np.arange(0, nsys, 1024))
+            assert per_system_relerr(m, sub.nsys, nrow, got, ref.D) <= tol
+
+
 def test_plan_mismatch_and_reuse(cuda):
     w = synth.dominant(3, 64, 12, seed=5, delta=2.0)
     a, b, c, d = to_dev(w.arrays, cuda)
@@ -211,15 +232,17 @@ def test_side_stream(cuda):
     assert per_system_relerr(5, 512, 32, D, ref.D) <= TOL
 
 
-FULL = [  # the production-size configurations: m, nsys, nrow, nseg, delta
-    (5, 65536, 256, 1, 1.2),
-    (5, 65536, 256, 16, 1.2),
-    (4, 256, 32768, 128, 1.2),
+FULL = [  # the production-size configurations: m, nsys, nrow, nseg, delta, keep the segments
+    (5, 65536, 256, 1, 1.2, False),
+    (5, 65536, 256, 16, 1.2, False),  # fills the GPU: solved one segment per line
+    (5, 65536, 256, 16, 1.2, True),   # the 16 segments kept (PBT_FLAG_REFERENCE_METHOD)
+    (4, 256, 32768, 128, 1.2, False),
 ]
 
 
-@pytest.mark.parametrize("m,nsys,nrow,nseg,delta", FULL, ids=["pencil_P1", "pencil_P16", "long_lines_P128"])
-def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta):
+@pytest.mark.parametrize("m,nsys,nrow,nseg,delta,segmented", FULL,
+                         ids=["pencil_P1", "pencil_P16", "pencil_P16_segmented", "long_lines_P128"])
+def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta, segmented):
     """Full batch on the GPU; 48 of its systems re-solved by the oracle.
     Systems are independent, so this checks those systems exactly."""
     w = synth.dominant(m, nsys, nrow, seed=2024, delta=delta)
@@ -227,7 +250,7 @@ def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta):
     pick = np.unique(np.concatenate([[0, nsys - 1], rng.choice(nsys, size=min(nsys, 46), replace=False)]))
     ref = oracle_solve(subset(w, pick), nseg)
     for prec, tol in PREC_TOL:
-        (_, _, _, D), singular = gpu_solve(w, nseg, precision=prec)
+        (_, _, _, D), singular = gpu_solve(w, nseg, precision=prec, reference_method=segmented)
         assert singular == 0
         got = column_subset(m, nsys, nrow, D, pick)
         err = per_system_relerr(m, len(pick), nrow, got, ref.D)
@@ -236,8 +259,8 @@ def test_full_size_against_oracle_subset(cuda, m, nsys, nrow, nseg, delta):
         assert np.isfinite(D).all()
 
 
-@pytest.mark.parametrize("nseg", [1, 2])
-def test_full_size_cyclic_against_oracle_subset(cuda, nseg):
+@pytest.mark.parametrize("nseg,segmented", [(1, False), (2, False), (2, True)])
+def test_full_size_cyclic_against_oracle_subset(cuda, nseg, segmented):
     """The pencil batch as periodic lines (m = 5, 65536 x 256, the bench's
     cyclic variant) on the GPU; 48 of its systems re-solved by the oracle's
     periodic solve (btdma_many_cycl restated)."""
@@ -247,7 +270,7 @@ def test_full_size_cyclic_against_oracle_subset(cuda, nseg):
     pick = np.unique(np.concatenate([[0, nsys - 1], rng.choice(nsys, size=46, replace=False)]))
     ref = oracle_solve(subset(w, pick), nseg, cyclic=True)
     for prec, tol in PREC_TOL:
-        (_, _, _, D), singular = gpu_solve(w, nseg, cyclic=True, precision=prec)
+        (_, _, _, D), singular = gpu_solve(w, nseg, cyclic=True, precision=prec, reference_method=segmented)
         assert singular == 0
         got = column_subset(m, nsys, nrow, D, pick)
         err = per_system_relerr(m, len(pick), nrow, got, ref.D)
