@@ -84,8 +84,9 @@ MIXED = [(1.05, 1), (1.05, 16), (1.5, 1), (1.5, 16)]  # (delta, nseg)
 # on the device), factors recomputed by the adjoint.
 ADJ = dict(m=4, nsys=16384, nrow=512, delta=1.5, segs=(8, 1), pressure_tiles=16)
 # Uneven batch: 32768 systems, N log-uniform in [16, 4096], m uniform in
-# {2, 3, 4, 5}, delta = 1.5; one persistent launch per sweep, 100 sweeps in a
-# CUDA graph; tuning by the autotuner; against one plain launch per (m, N).
+# {2, 3, 4, 5}, delta = 1.5; one persistent launch per block size and sweep,
+# 100 sweeps in a CUDA graph; tuning by the autotuner; against one uniform
+# plan per (m, power-of-two N bucket) with the systems padded to the bucket.
 UNEVEN = dict(nsys=32768, nmin=16, nmax=4096, mmin=2, mmax=5, delta=1.5, sweeps=100)
 # heat3d-style ADI step: a 512^3 field with a halo of 2, lines of 256 blocks of 2 points
 SHARED = dict(n=512, halo=2, sigma=0.05, steps=5)
@@ -258,50 +259,94 @@ def run_uneven(dev, log=None) -> dict:
         torch.cuda.synchronize()
         plan.status()
         t = e0.elapsed_time(e1) / 1e3 / u["sweeps"]
-        out[prec] = {"block_rows_per_s": rows / t, "ms_per_sweep": t * 1e3, "tuning": tuning, **plan.info()}
+        # The same sweeps launched one by one (no graph).
+        pa, pb, pc, pd = packed
+        e0.record()
+        for _ in range(5):
+            pd.copy_(d0)
+            plan.solve(pa, pb, pc, pd)
+        e1.record()
+        torch.cuda.synchronize()
+        plan.status()
+        te = e0.elapsed_time(e1) / 1e3 / 5
+        out[prec] = {"block_rows_per_s": rows / t, "ms_per_sweep": t * 1e3, "ms_per_sweep_no_graph": te * 1e3,
+                     "tuning": tuning, **plan.info()}
         plan.destroy()
         del packed, d0, g
-    # Plain launches: one uniform plan and one solve per distinct (m, N).
+    # The comparator a user of the plain plan API would build: one uniform plan
+    # per (m, N bucket), N buckets of powers of two, every system padded to its
+    # bucket's N with rows that decouple (B = I, A = C = 0, d = 0; the last
+    # real row's C zeroed, as the non-cyclic solve treats it).  The groups'
+    # solves run concurrently, one stream each, timed with CUDA events; one
+    # segment per line, or segments of ~256 rows for the long buckets.
+    import math
+
     groups = {}
     for s in range(u["nsys"]):
-        groups.setdefault((int(m[s]), int(n[s])), []).append(s)
-    plans, arrays = [], []
-    for (mm, nn), idx in groups.items():
-        k = len(idx)
-        def gather(src, off, per):
-            cols = [src[int(off[s]):int(off[s]) + per] for s in idx]
-            return torch.stack(cols, dim=1).reshape(-1).contiguous()   # (e, row) x sys -> reference layout
-        a_ = gather(user[0], mo, nn * mm * mm)
-        b_ = gather(user[1], mo, nn * mm * mm)
-        c_ = gather(user[2], mo, nn * mm * mm)
-        d_ = gather(user[3], vo, nn * mm)
-        plans.append(pbt.BtdmaGpuPlan().create(mm, k, nn, 1, precision="fp64"))
-        arrays.append((a_, b_, c_, d_, d_.clone(), mm, k, nn))
+        nb = 1 << max(1, math.ceil(math.log2(int(n[s]))))
+        groups.setdefault((int(m[s]), nb), []).append(s)
+    padded = []
+    for (mm, nb), idx in sorted(groups.items()):
+        blocks = [[], [], [], []]
+        for s in idx:
+            ns = int(n[s])
+            o, ov = int(mo[s]), int(vo[s])
+            a_ = user[0][o:o + ns * mm * mm].view(mm * mm, ns)
+            b_ = user[1][o:o + ns * mm * mm].view(mm * mm, ns)
+            c_ = user[2][o:o + ns * mm * mm].view(mm * mm, ns).clone()
+            d_ = user[3][ov:ov + ns * mm].view(mm, ns)
+            c_[:, ns - 1] = 0.0
+            pad = nb - ns
+            eye = torch.zeros(mm * mm, pad, dtype=torch.float64, device=dev)
+            eye[[i + mm * i for i in range(mm)], :] = 1.0
+            z2 = torch.zeros(mm * mm, pad, dtype=torch.float64, device=dev)
+            blocks[0].append(torch.cat([a_, z2], 1))
+            blocks[1].append(torch.cat([b_, eye], 1))
+            blocks[2].append(torch.cat([c_, z2], 1))
+            blocks[3].append(torch.cat([d_, torch.zeros(mm, pad, dtype=torch.float64, device=dev)], 1))
+        arrs = [torch.stack(bl, 2).contiguous().view(-1) for bl in blocks]  # (e, row, sys): reference layout
+        padded.append((mm, nb, len(idx), arrs))
     torch.cuda.synchronize()
+    padded_rows = sum(nb * k for _, nb, k, _ in padded)
+    main = torch.cuda.current_stream()
+    streams = [torch.cuda.Stream() for _ in padded]
+    for prec in ("fp64", "ff"):
+        for segmented in (False, True):
+            plans, work = [], []
+            for mm, nb, k, arrs in padded:
+                P = max(1, nb // 256) if segmented else 1
+                plans.append(pbt.BtdmaGpuPlan().create(mm, k, nb, P, precision=prec))
+                work.append(arrs[3].clone())
 
-    # One launch per (m, N) group, spread round-robin over 32 streams so the
-    # many small, latency-bound solves overlap (one stream serialises them
-    # into minutes per sweep).
-    streams = [torch.cuda.Stream() for _ in range(32)]
+            def sweep():
+                for pl, (mm, nb, k, arrs), w_, st in zip(plans, padded, work, streams):
+                    st.wait_stream(main)
+                    with torch.cuda.stream(st):
+                        w_.copy_(arrs[3])
+                        pbt.solve_noncyclic(pl, arrs[0], arrs[1], arrs[2], w_, mm, k, nb, stream=st)
+                for st in streams:
+                    main.wait_stream(st)
 
-    def sweep():
-        for i, (pl, (a_, b_, c_, d_, w_, mm, k, nn)) in enumerate(zip(plans, arrays)):
-            st = streams[i % len(streams)]
-            with torch.cuda.stream(st):
-                w_.copy_(d_)
-                pbt.solve_noncyclic(pl, a_, b_, c_, w_, mm, k, nn, stream=st)
-
-    sweep()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sweep()
-    torch.cuda.synchronize()
-    t = time.perf_counter() - t0
-    out["plain_per_m_n_fp64"] = {"block_rows_per_s": rows / t, "ms_per_sweep": t * 1e3, "launches": len(plans),
-                                 "streams": len(streams), "timing": "host wall clock, one sweep after one warm-up"}
-    for pl in plans:
-        pl.destroy()
-    del arrays, user
+            sweep()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 5
+            e0.record(main)
+            for _ in range(reps):
+                sweep()
+            e1.record(main)
+            torch.cuda.synchronize()
+            for pl in plans:
+                pl.status()
+                pl.destroy()
+            t = e0.elapsed_time(e1) / 1e3 / reps
+            key = f"grouped_plans_{prec}" + ("_segmented" if segmented else "")
+            out[key] = {"block_rows_per_s": rows / t, "ms_per_sweep": t * 1e3, "plans": len(padded),
+                        "padded_block_rows": padded_rows, "streams": len(streams),
+                        "nseg": "max(1, N_bucket // 256)" if segmented else 1}
+            del work
+    out["ff_over_fp64"] = out["fp64"]["ms_per_sweep"] / out["ff"]["ms_per_sweep"]
+    del padded, user
     torch.cuda.empty_cache()
     return out
 

@@ -1,6 +1,6 @@
 /*
  * pbt_batch.h -- uneven batches: thousands of block-tridiagonal systems of
- * different length N and block size m solved by one persistent launch
+ * different length N and block size m solved by persistent launches
  * (part of libpbt.so).  No counterpart in the reference, whose plan fixes
  * one (m, nsys, nrow) per call (pascal_btdma_cuda.hpp:128-145).
  *
@@ -11,7 +11,16 @@
  * N_s*m_s).  pbt_batch_pack rearranges such arrays into the batch's packed
  * layout (tiles of 32 systems of equal m, sorted by N); pbt_batch_solve works
  * on packed arrays; pbt_batch_unpack brings the solution back.  Non-cyclic
- * lines; A_0 and C_{N-1} of every system act as zero.
+ * lines; A_0 and C_{N-1} of every system act as zero.  In the packed layout a
+ * system shorter than its tile's longest is extended to that length with rows
+ * that decouple from it (B = I, A = C = 0, d = 0); unpack returns only the
+ * system's own rows.
+ *
+ * The solve runs, per block size present (largest total cost first), a
+ * persistent launch over the local-stage items, one warp per segmented
+ * tile for the reduced systems, and a persistent launch over the update
+ * items, all on the caller's stream; each launch carries one block size's
+ * code.
  *
  * Tuning (pbt_batch_tuning): the number of segments of each tile is
  * round(N_max / seg_len[m]) (one segment when seg_len[m] <= 0), so long lines
@@ -28,7 +37,7 @@
 extern "C" {
 #endif
 
-#define PBT_BATCH_MAX_BLOCK 5
+#define PBT_BATCH_MAX_BLOCK 10
 
 typedef struct pbt_batch pbt_batch;
 
@@ -65,19 +74,21 @@ int pbt_batch_pack(pbt_batch* batch, const double* ua, const double* ub, const d
 int pbt_batch_unpack(pbt_batch* batch, const double* pd, double* ud, void* stream);
 
 /* Solve every system of the batch in place on packed arrays: one memset of
- * the queue state and one persistent kernel, no host synchronisation. */
+ * the queue state and up to three launches per block size present, no host
+ * synchronisation. */
 int pbt_batch_solve(pbt_batch* batch, const double* pa, const double* pb, const double* pc, double* pd,
                     void* stream);
 
-/* Synchronises the last stream; reports zero pivots met and whether a wait
- * of the persistent kernel ran out (*timed_out = 1, the result is invalid).
- * Returns PBT_ECUDA (a wait ran out), PBT_ERANGE (a float-float batch left
- * the arithmetic's range, as pbt_plan_status; the result is invalid) or
- * PBT_ESINGULAR accordingly, in that order. */
+/* Synchronises the last stream; reports zero pivots met.  *timed_out is
+ * always 0: the stages are separate launches, so no kernel waits on another
+ * (the argument stays for callers of the earlier single-launch form).
+ * Returns PBT_ERANGE (a float-float batch left the arithmetic's range, as
+ * pbt_plan_status; the result is invalid) or PBT_ESINGULAR accordingly, in
+ * that order. */
 int pbt_batch_status(pbt_batch* batch, long long* nsingular, int* timed_out);
 
-/* Shape of the schedule: tiles, stage-1 and stage-3 items, persistent CTAs of
- * the last solve (0 before the first). */
+/* Shape of the schedule: tiles, stage-1 and stage-3 items, CTAs of the
+ * largest persistent launch of the last solve (0 before the first). */
 int pbt_batch_info(const pbt_batch* batch, int* ntiles, int* n_items1, int* n_items3, int* grid_ctas);
 
 #ifdef __cplusplus

@@ -1,11 +1,11 @@
 """Uneven batches (include/pbt_batch.h): many systems of different length N
-and block size m solved by one persistent kernel launch, plus the autotuner
+and block size m (1..10) solved by one persistent kernel launch per block size, plus the autotuner
 that picks the segmentation and CTA shape per (m, N, nsys) bucket, and CUDA
 graph capture of repeated sweeps.
 
     plan = BatchPlan(m_per_sys, n_per_sys, precision="fp64", tuning=autotune(...))
     pa, pb, pc, pd = plan.pack(ua, ub, uc, ud)      # per-system -> packed (device tensors)
-    plan.solve(pa, pb, pc, pd)                      # one persistent launch
+    plan.solve(pa, pb, pc, pd)                      # one persistent launch per block size
     ud = plan.unpack(pd)                            # packed -> per-system
 
 Per-system (caller) layout: system s is the reference layout of one system at
@@ -25,7 +25,7 @@ import numpy as np
 from . import _native as N
 from . import _raise
 
-PBT_BATCH_MAX_BLOCK = 5
+PBT_BATCH_MAX_BLOCK = 10
 
 
 class BatchTuning(C.Structure):
@@ -170,7 +170,7 @@ class BatchPlan:
 # ---------------------------------------------------------------------------
 # Autotuner.
 # ---------------------------------------------------------------------------
-SEG_CANDIDATES = (0, 1024, 512, 256, 128)   # 0: one segment per line
+SEG_CANDIDATES = (0, 1024, 512, 256, 128, 64, 32)   # 0: one segment per line
 WARP_CANDIDATES = (4, 2)
 
 

@@ -38,8 +38,8 @@ MAX_BLOCK = 10
 
 # Families of kernels instantiated per block size: (source, object stem).
 PER_M_SOURCES = [("pbt_inst.cu", "F64"), ("pbt_inst.cu", "FF"), ("pbt_inst.cu", "F32")]
-HOST_SOURCES = ["pbt_api.cpp", "pbt_noalloc.cu", "pbt_batch.cpp", "pbt_batch_f64.cu",
-                "pbt_batch_ff.cu", "pbt_layout.cu", "pbt_shared.cu"]
+HOST_SOURCES = ["pbt_api.cpp", "pbt_noalloc.cu", "pbt_batch.cpp", "pbt_batch_pack.cu", "pbt_layout.cu",
+                "pbt_shared.cu"]
 
 
 def _nvcc() -> str:
@@ -85,7 +85,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
             obj = BUILD / f"{stem.lower()}_m{m}.o"
             objs.append(obj)
             if _stale(obj, [CSRC / src] + hdrs):
-                extra = ["-DPBT_NUM_IS_F64"] if stem == "F64" else []
+                extra = {"F64": ["-DPBT_NUM_IS_F64"], "FF": ["-DPBT_NUM_IS_FF"]}.get(stem, [])
                 tasks.append((obj, [nvcc, *NVCC_FLAGS, f"-DPBT_M={m}", f"-DPBT_NUM=pbt::{stem}", *extra, "-c",
                                     str(CSRC / src), "-o", str(obj)]))
     for src in HOST_SOURCES:

@@ -16,6 +16,12 @@
 
 struct pbt_batch {
     int nsys = 0, precision = 0, ntiles = 0, n1 = 0, n3 = 0, warps = 4, last_grid = 0;
+    // Items of block size m: items1[off1[m] .. off1[m] + cnt1[m]), likewise
+    // items3; one persistent launch per block size present, in `order`.
+    int off1[PBT_MAX_BLOCK + 1] = {}, cnt1[PBT_MAX_BLOCK + 1] = {};
+    int off3[PBT_MAX_BLOCK + 1] = {}, cnt3[PBT_MAX_BLOCK + 1] = {};
+    int offr[PBT_MAX_BLOCK + 1] = {}, cntr[PBT_MAX_BLOCK + 1] = {};
+    std::vector<int> order;
     std::vector<long long> user_mat_off, user_vec_off;
     long long user_mat = 0, user_vec = 0, packed_mat = 0, packed_vec = 0, red_mat = 0, red_vec = 0;
     // device
@@ -24,11 +30,12 @@ struct pbt_batch {
     int* sys_of = nullptr;
     int2* items1 = nullptr;
     int2* items3 = nullptr;
+    int* red_tiles = nullptr;
     long long* d_user_mat_off = nullptr;
     long long* d_user_vec_off = nullptr;
     long long* row_start = nullptr;
     long long pack_total = 0;
-    int* state = nullptr;  // head1, head3, error, pad, seg_done[ntiles], ready[ntiles]
+    int* state = nullptr;  // error (always 0), pad, head1[m], head3[m] (kHeads each)
     unsigned long long* status = nullptr;
     double *aw = nullptr, *cw = nullptr, *ra = nullptr, *rc = nullptr, *rd = nullptr;
     cudaStream_t last_stream = nullptr;
@@ -38,6 +45,34 @@ struct pbt_batch {
 namespace {
 
 constexpr unsigned kBatchMagic = 0x50425442u;
+constexpr int kHeads = PBT_MAX_BLOCK + 1;
+
+size_t state_ints(int) { return (size_t)2 + 2 * kHeads; }
+
+// One launch of the batch kernel for block size m (pbt_inst.cu instantiates
+// launch_batch per arithmetic and block size).
+cudaError_t launch_m(int precision, int m, const pbt::BatchArgs& ba, int warps, cudaStream_t s, int* grid) {
+#define PBT_BATCH_CASE(MM)                                                                        \
+    case MM:                                                                                      \
+        return precision == PBT_PREC_FF ? pbt::launch_batch<pbt::FF, MM>(ba, warps, s, grid)    \
+                                        : pbt::launch_batch<pbt::F64, MM>(ba, warps, s, grid);
+    switch (m) {
+        PBT_BATCH_CASE(1)
+        PBT_BATCH_CASE(2)
+        PBT_BATCH_CASE(3)
+        PBT_BATCH_CASE(4)
+        PBT_BATCH_CASE(5)
+        PBT_BATCH_CASE(6)
+        PBT_BATCH_CASE(7)
+        PBT_BATCH_CASE(8)
+        PBT_BATCH_CASE(9)
+        PBT_BATCH_CASE(10)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef PBT_BATCH_CASE
+}
+static_assert(PBT_BATCH_MAX_BLOCK == 10, "launch_m lists block sizes 1..10");
 
 int bfail(int code, const std::string& msg) { return pbt::set_last_error(code, msg.c_str()); }
 
@@ -65,6 +100,7 @@ int dalloc(double** p, long long n) {
 }
 
 void free_batch(pbt_batch* b) {
+    cudaFree(b->red_tiles);
     cudaFree(b->tiles);
     cudaFree(b->lane_rows);
     cudaFree(b->sys_of);
@@ -153,12 +189,13 @@ int pbt_batch_create(pbt_batch** out, int nsys, const int* m, const int* nrow, i
         t.m = mm;
         t.lanes = lanes;
         t.rows = nrow[order[k]];
-        const int nmin = nrow[order[k + lanes - 1]];
+        // Systems are padded to the tile's rows (pbt_batch_pack), so the
+        // segments split t.rows.
         int P = 1;
         const int L = tu.seg_len[mm];
         if (L > 0) {
             P = (t.rows + L / 2) / L;
-            P = std::max(1, std::min(P, nmin / 3));
+            P = std::max(1, std::min(P, t.rows / 3));
         }
         t.nseg = P;
         t.mat_off = mat_off;
@@ -186,45 +223,71 @@ int pbt_batch_create(pbt_batch** out, int nsys, const int* m, const int* nrow, i
     b->red_mat = red_m;
     b->red_vec = red_v;
     b->pack_total = rowacc;
-    // Work items.  Stage 1 by decreasing cost (m^3 * rows of the item; the
-    // two-stage elimination costs ~2.4x block Thomas per row).
+    // Work items, per block size.  Stage 1 by decreasing cost (m^3 * rows of
+    // the item; the two-stage elimination costs ~2.4x block Thomas per row);
+    // stage 3 in the order stage 1 first reaches each tile.  The launches run
+    // the block sizes in decreasing total cost.
     struct It {
         int t, s;
         double cost;
     };
-    std::vector<It> it1;
-    for (int t = 0; t < b->ntiles; ++t) {
-        const auto& tl = tiles[t];
-        const double w = (double)tl.m * tl.m * tl.m;
-        if (tl.nseg == 1) {
-            it1.push_back({t, -1, w * tl.rows});
-        } else {
-            for (int sg = 0; sg < tl.nseg; ++sg) it1.push_back({t, sg, 2.4 * w * tl.rows / tl.nseg});
-        }
-    }
-    std::stable_sort(it1.begin(), it1.end(), [](const It& x, const It& y) { return x.cost > y.cost; });
     std::vector<int2> items1, items3;
+    std::vector<int> red_tiles;
     std::vector<char> seen(b->ntiles, 0);
-    for (const auto& i : it1) {
-        items1.push_back(make_int2(i.t, i.s));
-        if (i.s >= 0 && !seen[i.t]) {
-            seen[i.t] = 1;
-            for (int sg = 0; sg < tiles[i.t].nseg; ++sg) items3.push_back(make_int2(i.t, sg));
+    std::vector<std::pair<double, int>> by_cost;
+    for (int mm = 1; mm <= PBT_BATCH_MAX_BLOCK; ++mm) {
+        std::vector<It> it1;
+        double total = 0.0;
+        for (int t = 0; t < b->ntiles; ++t) {
+            const auto& tl = tiles[t];
+            if (tl.m != mm) continue;
+            const double w = (double)tl.m * tl.m * tl.m;
+            if (tl.nseg == 1) {
+                it1.push_back({t, -1, w * tl.rows});
+            } else {
+                for (int sg = 0; sg < tl.nseg; ++sg) it1.push_back({t, sg, 2.4 * w * tl.rows / tl.nseg});
+            }
+            total += it1.back().cost * (tl.nseg == 1 ? 1 : tl.nseg);
         }
+        if (it1.empty()) continue;
+        std::stable_sort(it1.begin(), it1.end(), [](const It& x, const It& y) { return x.cost > y.cost; });
+        b->off1[mm] = (int)items1.size();
+        b->off3[mm] = (int)items3.size();
+        for (const auto& i : it1) {
+            items1.push_back(make_int2(i.t, i.s));
+            if (i.s >= 0 && !seen[i.t]) {
+                seen[i.t] = 1;
+                for (int sg = 0; sg < tiles[i.t].nseg; ++sg) items3.push_back(make_int2(i.t, sg));
+            }
+        }
+        b->cnt1[mm] = (int)items1.size() - b->off1[mm];
+        b->cnt3[mm] = (int)items3.size() - b->off3[mm];
+        // Reduced solves, longest first.
+        b->offr[mm] = (int)red_tiles.size();
+        for (int t = 0; t < b->ntiles; ++t)
+            if (tiles[t].m == mm && tiles[t].nseg > 1) red_tiles.push_back(t);
+        std::stable_sort(red_tiles.begin() + b->offr[mm], red_tiles.end(),
+                         [&](int x, int y) { return tiles[x].nseg > tiles[y].nseg; });
+        b->cntr[mm] = (int)red_tiles.size() - b->offr[mm];
+        by_cost.push_back({total, mm});
     }
+    std::stable_sort(by_cost.begin(), by_cost.end(), [](const std::pair<double, int>& x, const std::pair<double, int>& y) {
+        return x.first > y.first;
+    });
+    for (const auto& c : by_cost) b->order.push_back(c.second);
     b->n1 = (int)items1.size();
     b->n3 = (int)items3.size();
     int rc = PBT_OK;
     if ((rc = upload(&b->tiles, tiles)) || (rc = upload(&b->lane_rows, lane_rows)) || (rc = upload(&b->sys_of, sys_of)) ||
-        (rc = upload(&b->items1, items1)) || (rc = upload(&b->items3, items3)) ||
+        (rc = upload(&b->items1, items1)) || (rc = upload(&b->items3, items3)) || (rc = upload(&b->red_tiles, red_tiles)) ||
         (rc = upload(&b->d_user_mat_off, b->user_mat_off)) || (rc = upload(&b->d_user_vec_off, b->user_vec_off)) ||
         (rc = upload(&b->row_start, row_start)))
         goto fail_out;
     {
-        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&b->state), sizeof(int) * (4 + 2 * (size_t)b->ntiles));
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&b->state), sizeof(int) * state_ints(b->ntiles));
         if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->status), sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMemset(b->status, 0, sizeof(unsigned long long));
-        if (e == cudaSuccess) e = cudaMemset(b->state, 0, sizeof(int) * (4 + 2 * (size_t)b->ntiles));
+        if (e == cudaSuccess) e = cudaMemset(b->state, 0, sizeof(int) * state_ints(b->ntiles));
         if (e != cudaSuccess) {
             rc = bcuda(e, "batch_create: queue state");
             goto fail_out;
@@ -308,7 +371,7 @@ int pbt_batch_solve(pbt_batch* b, const double* pa, const double* pb, const doub
     if (!pa || !pb || !pc || !pd) return bfail(PBT_EINVAL, "batch_solve: null pointer");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     b->last_stream = s;
-    cudaError_t e = cudaMemsetAsync(b->state, 0, sizeof(int) * (4 + 2 * (size_t)b->ntiles), s);
+    cudaError_t e = cudaMemsetAsync(b->state, 0, sizeof(int) * state_ints(b->ntiles), s);
     if (e != cudaSuccess) return bcuda(e, "batch_solve: queue reset");
     pbt::BatchArgs ba;
     ba.a = pa;
@@ -322,20 +385,23 @@ int pbt_batch_solve(pbt_batch* b, const double* pa, const double* pb, const doub
     ba.rd = b->rd;
     ba.tiles = b->tiles;
     ba.lane_rows = b->lane_rows;
-    ba.items1 = b->items1;
-    ba.items3 = b->items3;
-    ba.n1 = b->n1;
-    ba.n3 = b->n3;
-    ba.head1 = b->state;
-    ba.head3 = b->state + 1;
-    ba.error = b->state + 2;
-    ba.seg_done = b->state + 4;
-    ba.ready = b->state + 4 + b->ntiles;
     ba.status = b->status;
-    ba.spin_limit = 1LL << 24;  // x 256 ns sleeps: a wait gives up after ~4 s
-    e = b->precision == PBT_PREC_FF ? pbt::launch_batch<pbt::FF>(ba, b->warps, s, &b->last_grid)
-                                    : pbt::launch_batch<pbt::F64>(ba, b->warps, s, &b->last_grid);
-    return e == cudaSuccess ? PBT_OK : bcuda(e, "batch_solve: launch");
+    b->last_grid = 0;
+    for (int mm : b->order) {
+        ba.items1 = b->items1 + b->off1[mm];
+        ba.items3 = b->items3 + b->off3[mm];
+        ba.red_tiles = b->red_tiles + b->offr[mm];
+        ba.n1 = b->cnt1[mm];
+        ba.n3 = b->cnt3[mm];
+        ba.n_red = b->cntr[mm];
+        ba.head1 = b->state + 2 + mm;
+        ba.head3 = b->state + 2 + kHeads + mm;
+        int grid = 0;
+        e = launch_m(b->precision, mm, ba, b->warps, s, &grid);
+        if (e != cudaSuccess) return bcuda(e, "batch_solve: launch");
+        b->last_grid = std::max(b->last_grid, grid);
+    }
+    return PBT_OK;
 }
 
 int pbt_batch_status(pbt_batch* b, long long* nsingular, int* timed_out) {
@@ -346,7 +412,7 @@ int pbt_batch_status(pbt_batch* b, long long* nsingular, int* timed_out) {
     unsigned long long v = 0;
     int err = 0;
     if ((e = cudaMemcpy(&v, b->status, sizeof v, cudaMemcpyDeviceToHost)) != cudaSuccess ||
-        (e = cudaMemcpy(&err, b->state + 2, sizeof err, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+        (e = cudaMemcpy(&err, b->state, sizeof err, cudaMemcpyDeviceToHost)) != cudaSuccess ||
         (e = cudaMemset(b->status, 0, sizeof v)) != cudaSuccess)
         return bcuda(e, "batch_status: read");
     const unsigned long long pivots = v & pbt::kPivotCountMask;

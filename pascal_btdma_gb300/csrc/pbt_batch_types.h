@@ -31,14 +31,11 @@ struct BatchArgs {
     const int* lane_rows;  // [tile*32 + lane]: N of that system, 0 for an empty lane
     const int2* items1;    // (tile, segment or -1 for a whole-line Thomas item)
     const int2* items3;    // (tile, segment)
-    int n1, n3;
-    int* head1;            // queue heads, zeroed before every launch
+    const int* red_tiles;  // the segmented tiles
+    int n1, n3, n_red;
+    int* head1;            // queue heads, zeroed before every solve
     int* head3;
-    int* seg_done;         // per tile, zeroed before every launch
-    int* ready;            // per tile, zeroed before every launch
-    int* error;            // 1 = a wait ran out
-    unsigned long long* status;  // zero pivots
-    long long spin_limit;
+    unsigned long long* status;  // zero pivots, range flag
 };
 
 // Packing between the caller's per-system layout and the tiled layout.
@@ -53,7 +50,9 @@ struct PackArgs {
     long long total;                // sum over tiles of 32*rows
 };
 
-template <class Num>
+// The launches of block size M (pbt_batch.cuh; instantiated with the other
+// kernels of (Num, M) in pbt_inst.cu).
+template <class Num, int M>
 cudaError_t launch_batch(const BatchArgs& ba, int warps, cudaStream_t s, int* grid_out);
 cudaError_t launch_pack(const PackArgs& pa, const double* ua, const double* ub, const double* uc, const double* ud,
                         double* ta, double* tb, double* tc, double* td, double* ud_out, int dir, cudaStream_t s);

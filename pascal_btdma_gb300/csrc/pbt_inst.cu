@@ -14,6 +14,9 @@
 #if PBT_M <= 6
 #include "pbt_staged.cuh"
 #endif
+#if defined(PBT_NUM_IS_F64) || defined(PBT_NUM_IS_FF)
+#include "pbt_batch.cuh"
+#endif
 
 namespace pbt {
 template cudaError_t launch_thomas<PBT_NUM, PBT_M>(const SolveArgs&);
@@ -27,6 +30,9 @@ template cudaError_t launch_reduced<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_reduced_cyclic<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_update<PBT_NUM, PBT_M>(const SolveArgs&);
 template cudaError_t launch_adjoint<PBT_NUM, PBT_M>(const SolveArgs&, const AdjointArgs&);
+#if defined(PBT_NUM_IS_F64) || defined(PBT_NUM_IS_FF)
+template cudaError_t launch_batch<PBT_NUM, PBT_M>(const BatchArgs&, int, cudaStream_t, int*);
+#endif
 #ifdef PBT_NUM_IS_F64
 template cudaError_t launch_transpose_blocks<PBT_M>(const SolveArgs&, double*, double*, double*);
 template cudaError_t launch_gradients<PBT_M>(const SolveArgs&, const AdjointArgs&);

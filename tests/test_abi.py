@@ -59,8 +59,8 @@ def test_batch_create_rejects_without_gpu():
 
     from pascal_btdma_gb300 import batch
 
-    with pytest.raises(ValueError, match="m=7"):
-        batch.BatchPlan(np.array([2, 7]), np.array([10, 10]))
+    with pytest.raises(ValueError, match="m=11"):
+        batch.BatchPlan(np.array([2, 11]), np.array([10, 10]))
     with pytest.raises(ValueError, match="equal length"):
         batch.BatchPlan(np.array([2, 3]), np.array([10]))
 

@@ -44,9 +44,11 @@ def check(m, n, got, ref, tol):
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("ff", 1e-12)])
 @pytest.mark.parametrize("seg", [0, 32, 256])
-def test_batch_matches_oracle(cuda, prec, tol, seg):
-    m, n, systems, user = make_batch(300, 2, 700, seed=3)
-    plan = B.BatchPlan(m, n, prec, {"seg_len": {k: seg for k in range(1, 6)}, "warps_per_cta": 4})
+@pytest.mark.parametrize("mmax", [5, 10])
+def test_batch_matches_oracle(cuda, prec, tol, seg, mmax):
+    """Every system against the oracle; block sizes 1..5, and 1..10."""
+    m, n, systems, user = make_batch(300, 2, 700, seed=3 + mmax, mmax=mmax)
+    plan = B.BatchPlan(m, n, prec, {"seg_len": {k: seg for k in range(1, 11)}, "warps_per_cta": 4})
     um, uv, pm, pv = plan.sizes()
     assert um == sum(int(mm * mm * nn) for mm, nn in zip(m, n)) and uv == sum(int(mm * nn) for mm, nn in zip(m, n))
     ua, ub, uc, ud = (torch.from_numpy(x).to(cuda) for x in user)
@@ -57,6 +59,7 @@ def test_batch_matches_oracle(cuda, prec, tol, seg):
     check(m, n, got, reference(systems), tol)
     info = plan.info()
     assert info["tiles"] >= 300 // 32 and info["grid_ctas"] > 0
+    assert set(np.unique(m)) == set(range(1, mmax + 1))
     if seg == 32:
         assert info["stage3_items"] > 0  # long lines were segmented
     plan.destroy()
@@ -73,7 +76,7 @@ def test_batch_user_offsets_and_layout(cuda):
 
 def test_batch_graph_replay(cuda):
     m, n, systems, user = make_batch(200, 2, 400, seed=5)
-    plan = B.BatchPlan(m, n, "fp64", {"seg_len": {k: 64 for k in range(1, 6)}, "warps_per_cta": 4})
+    plan = B.BatchPlan(m, n, "fp64", {"seg_len": {k: 64 for k in range(1, 11)}, "warps_per_cta": 4})
     ua, ub, uc, ud = (torch.from_numpy(x).to(cuda) for x in user)
     packed = plan.pack(ua, ub, uc, ud)
     d0 = packed[3].clone()
@@ -102,8 +105,8 @@ def test_batch_autotune(cuda, tmp_path):
 
 
 def test_batch_rejects_bad_shapes(cuda):
-    with pytest.raises(ValueError, match="m=6"):
-        B.BatchPlan([2, 6], [10, 10], "fp64")
+    with pytest.raises(ValueError, match="m=11"):
+        B.BatchPlan([2, 11], [10, 10], "fp64")
     with pytest.raises(ValueError, match="nrow=1"):
         B.BatchPlan([2, 3], [10, 1], "fp64")
     with pytest.raises(NotImplementedError):
