@@ -896,6 +896,44 @@ def run_case(args):
                       "algorithmic_gbs": rows * bytes_per_row(m) * args.steps / t / 1e9}), flush=True)
 
 
+def run_batch_case(args):
+    """The bench's uneven batch restricted to one block size, for profiler
+    captures: --batch-case m,seg_len[,precision] runs W + K sweeps (D restored
+    before each) and prints ms per sweep.  Not a bench line."""
+    import torch
+
+    from pascal_btdma_gb300 import batch as B
+    from pascal_btdma_gb300 import synth
+
+    parts = args.batch_case.split(",")
+    mm, seg = int(parts[0]), int(parts[1])
+    prec = parts[2] if len(parts) > 2 else "ff"
+    u = UNEVEN
+    n_all, m_all = synth.uneven_shapes(SEED, u["nsys"], u["nmin"], u["nmax"], u["mmin"], u["mmax"])
+    sel = m_all == mm
+    m, n = m_all[sel], n_all[sel]
+    A, Bm, Cm, D, _, _ = synth.fill_batch(m, n, seed=SEED, delta=u["delta"])
+    user = tuple(torch.from_numpy(x).to("cuda") for x in (A, Bm, Cm, D))
+    plan = B.BatchPlan(m, n, prec, {"seg_len": {mm: seg}, "warps_per_cta": 4})
+    pa, pb, pc, pd = plan.pack(*user)
+    d0 = pd.clone()
+    for _ in range(args.warmup):
+        pd.copy_(d0)
+        plan.solve(pa, pb, pc, pd)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        pd.copy_(d0)
+        plan.solve(pa, pb, pc, pd)
+    e1.record()
+    torch.cuda.synchronize()
+    plan.status()
+    print(json.dumps({"batch_case": {"m": mm, "seg_len": seg, "precision": prec, "systems": int(sel.sum()),
+                                     "block_rows": int(n.sum())}, **plan.info(),
+                      "ms_per_sweep": e0.elapsed_time(e1) / args.steps}), flush=True)
+    plan.destroy()
+
+
 def run_reference(args):
     """The reference algorithm's CPU path on the host cores, a bounded sample per step."""
     ws, rank, _ = dist_info()
@@ -948,9 +986,14 @@ def main():
                          "uneven, shared, lines, cpu; 'all' (default) or 'main' (headline only)")
     ap.add_argument("--case", default="",
                     help="m,nsys,nrow,nseg[,cyclic][,precision]: time one workload only (profiler captures)")
+    ap.add_argument("--batch-case", default="",
+                    help="m,seg_len[,precision]: the uneven batch's systems of block size m only (profiler captures)")
     args = ap.parse_args()
     if args.case:
         run_case(args)
+        return
+    if args.batch_case:
+        run_batch_case(args)
         return
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
