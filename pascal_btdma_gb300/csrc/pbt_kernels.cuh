@@ -486,6 +486,20 @@ template <class Num>
 __host__ __device__ constexpr bool lu_rolled() {
     return Num::kConv;
 }
+// Variants of the rolled float-float row, chosen by measurement (GB300,
+// pencil batch m = 5): the d column solved inside the C-column loop as its
+// first column, one copy of the column solve's code less (PBT_LU_MERGE_Y:
+// 6.25 -> 5.93 ms); the C-column loop unrolled by 2 (6.79 ms) or the
+// A-column loop by 2 or 5 (6.50 / 6.43 ms) lose.
+#ifndef PBT_LU_MERGE_Y
+#define PBT_LU_MERGE_Y 1
+#endif
+#ifndef PBT_LU_COL_UNROLL
+#define PBT_LU_COL_UNROLL 1
+#endif
+#ifndef PBT_LU_K_UNROLL
+#define PBT_LU_K_UNROLL 1
+#endif
 template <class Num, int M>
 __host__ __device__ constexpr bool lu_prefetch_c() {
     return M == 5 && Num::kConv;
@@ -559,7 +573,8 @@ PBT_UNROLL
 PBT_UNROLL
                 for (int i = 0; i < M; ++i, pa += plane) an[i] = __ldg(pa);
             }
-#pragma unroll(lu_rolled<Num>() ? 1 : M)
+            constexpr int kKUnroll = lu_rolled<Num>() ? PBT_LU_K_UNROLL : M;
+#pragma unroll(kKUnroll)
             for (int k = 0; k < M; ++k) {
                 T ck[M];
 PBT_UNROLL
@@ -596,6 +611,71 @@ PBT_UNROLL
         }
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
+#if PBT_LU_MERGE_Y
+        // y as column -1 of the rolled column loop (one copy of the column
+        // solve's code for y and C).
+        if constexpr (lu_rolled<Num>()) {
+            const size_t plane = opaque(plane0);
+            const double* pc = C + o;
+            double* pw = CW + o;
+            auto ld_c = [&](const double* p) -> double { return (lu_ldg<M>() && raw) ? __ldg(p) : *p; };
+            double nxt[M];
+            if (lu_prefetch_c<Num, M>() && !last) {
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pc += plane) nxt[i] = ld_c(pc);
+            }
+            const int jend = last ? 0 : M;
+#pragma unroll 1
+            for (int j = -1; j < jend; ++j) {
+                Acc cj[M];
+                T xj[M];
+                if (j < 0) {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) cj[i] = xd[i];
+                } else if constexpr (lu_prefetch_c<Num, M>()) {
+                    double cur[M];
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) cur[i] = nxt[i];
+                    if (j + 1 < M) {
+PBT_UNROLL
+                        for (int i = 0; i < M; ++i, pc += plane) nxt[i] = ld_c(pc);
+                    }
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) cj[i] = Num::acc(Num::in(&cur[i]));
+                } else {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i, pc += plane) {
+                        const double v = ld_c(pc);
+                        cj[i] = Num::acc(Num::in(&v));
+                    }
+                }
+                lu_solve<Num, M>(lu, cj, xj);
+                if (j < 0) {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) {
+                        y[i] = xj[i];
+                        Num::sts(cps + (M * M + i) * cstride, xj[i]);
+                    }
+                } else {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i, pw += plane) {
+                        if (raw || !Num::kConv)
+                            Num::sts(pw, xj[i]);
+                        else
+                            Num::out(pw, xj[i]);
+                        Num::sts(cps + (i * M + j) * cstride, xj[i]);
+                    }
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+            if (last) {
+                out_vec<Num, M>(D + o, plane, y, amax);
+                break;
+            }
+            st_raw_vec<Num, M>(D + o, plane, y);
+            continue;
+        }
+#endif
         lu_solve<Num, M>(lu, xd, y);
         if constexpr (lu_rolled<Num>()) {
 PBT_UNROLL
@@ -623,7 +703,8 @@ PBT_UNROLL
 PBT_UNROLL
             for (int i = 0; i < M; ++i, pc += plane) nxt[i] = ld_c(pc);
         }
-#pragma unroll(lu_rolled<Num>() ? 1 : M)
+        constexpr int kColUnroll = lu_rolled<Num>() ? PBT_LU_COL_UNROLL : M;
+#pragma unroll(kColUnroll)
         for (int j = 0; j < M; ++j) {
             Acc cj[M];
             T xj[M];
@@ -879,7 +960,9 @@ PBT_UNROLL
         // The 2m right-hand-side columns in one rolled loop (one copy of the
         // column solve's code): jj < m, column jj of e_q - W (e_q = -C_{N-1}
         // on the last row, else 0) into EW and the e slots; jj >= m, column
-        // jj - m of C_q into CW and the C' slots (not on the last row).
+        // jj - m of C_q into CW and the C' slots (not on the last row).  y
+        // keeps its own solve: inside the loop it measured slower here (the
+        // pencil batch as periodic lines, float-float: 14.79 vs 14.07 ms).
         {
             const size_t plane = opaque(plane0);
             const int ncol = last ? M : 2 * M;
@@ -1353,22 +1436,22 @@ PBT_UNROLL
         }
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
-        lu_solve<Num, M>(lu, xd, y);
-PBT_UNROLL
-        for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
-        st_raw_vec<Num, M>(D + o, opaque(plane0), y);
-        // jj < m: column jj of A' (right-hand side A on rows 0, 1, else -W);
-        // jj >= m: column jj - m of C'.
+        // jj = -1: d'; jj < m: column jj of A' (right-hand side A on rows 0,
+        // 1, else -W); jj >= m: column jj - m of C'.  One rolled loop, one
+        // copy of the column solve's code.
         {
             const size_t plane = opaque(plane0);
 #pragma unroll 1
-            for (int jj = 0; jj < 2 * M; ++jj) {
+            for (int jj = -1; jj < 2 * M; ++jj) {
                 const bool acol = jj < M;
                 const int j = acol ? jj : jj - M;
                 const size_t co = o + (size_t)(M * j) * plane;
                 Acc v[M];
                 T xj[M];
-                if (acol && !first2) {
+                if (jj < 0) {
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) v[i] = xd[i];
+                } else if (acol && !first2) {
 PBT_UNROLL
                     for (int i = 0; i < M; ++i) v[i] = Num::acc(Num::neg(Num::lds(slot(kE + i * M + j))));
                 } else {
@@ -1377,12 +1460,21 @@ PBT_UNROLL
                     for (int i = 0; i < M; ++i) v[i] = Num::acc(Num::in(ps + (size_t)i * plane));
                 }
                 lu_solve<Num, M>(lu, v, xj);
-                double* pw = (acol ? AW : CW) + co;
-                const int s0 = acol ? kE + j : j;
+                if (jj < 0) {
 PBT_UNROLL
-                for (int i = 0; i < M; ++i) {
-                    st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
-                    Num::sts(slot(s0 + i * M), xj[i]);
+                    for (int i = 0; i < M; ++i) {
+                        y[i] = xj[i];
+                        Num::sts(slot(kY + i), xj[i]);
+                    }
+                    st_raw_vec<Num, M>(D + o, plane, y);
+                } else {
+                    double* pw = (acol ? AW : CW) + co;
+                    const int s0 = acol ? kE + j : j;
+PBT_UNROLL
+                    for (int i = 0; i < M; ++i) {
+                        st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
+                        Num::sts(slot(s0 + i * M), xj[i]);
+                    }
                 }
                 if (PBT_ROW_FENCE) mem_fence_compiler();
             }
@@ -1514,12 +1606,10 @@ PBT_UNROLL
         }
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
-        lu_solve<Num, M>(lu, xd, y);
-        st_raw_vec<Num, M>(D, plane, y);
         const size_t ro = rrs * (size_t)(2 * seg);
-        st_raw_vec<Num, M>(RD + ro, rplane, y);
+        // jj = -1: d'_0; then the A' and C' columns, as in the forward sweep.
 #pragma unroll 1
-        for (int jj = 0; jj < 2 * M; ++jj) {
+        for (int jj = -1; jj < 2 * M; ++jj) {
             const bool acol = jj < M;
             const int j = acol ? jj : jj - M;
             double* pw = (acol ? AW : CW) + (size_t)(M * j) * plane;
@@ -1527,14 +1617,20 @@ PBT_UNROLL
             T xj[M];
 PBT_UNROLL
             for (int i = 0; i < M; ++i)
-                v[i] = acol ? Num::acc(ld_fac<Num>(pw + (size_t)i * plane, raw))
-                            : Num::acc(Num::neg(Num::lds(slot(j + i * M))));
+                v[i] = jj < 0 ? xd[i]
+                              : (acol ? Num::acc(ld_fac<Num>(pw + (size_t)i * plane, raw))
+                                      : Num::acc(Num::neg(Num::lds(slot(j + i * M)))));
             lu_solve<Num, M>(lu, v, xj);
-            double* pr = (acol ? RA : RC) + ro + (size_t)(M * j) * rplane;
+            if (jj < 0) {
+                st_raw_vec<Num, M>(D, plane, xj);
+                st_raw_vec<Num, M>(RD + ro, rplane, xj);
+            } else {
+                double* pr = (acol ? RA : RC) + ro + (size_t)(M * j) * rplane;
 PBT_UNROLL
-            for (int i = 0; i < M; ++i) {
-                st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
-                Num::sts(pr + (size_t)i * rplane, xj[i]);
+                for (int i = 0; i < M; ++i) {
+                    st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
+                    Num::sts(pr + (size_t)i * rplane, xj[i]);
+                }
             }
             if (PBT_ROW_FENCE) mem_fence_compiler();
         }
