@@ -869,7 +869,7 @@ def run_ours(args):
 
 def run_case(args):
     """One workload, for profiler captures and size sweeps: --case
-    m,nsys,nrow,nseg[,cyclic][,precision] runs W + K solves of it on cuda:0
+    m,nsys,nrow,nseg[,cyclic][,precision][,segmented] runs W + K solves of it on cuda:0
     (each on a fresh right-hand side) and prints ms per solve.  Not a bench
     line: the headline and its sections are run_ours."""
     import torch
@@ -881,17 +881,18 @@ def run_case(args):
     m, nsys, nrow, nseg = (int(x) for x in parts[:4])
     cyclic = len(parts) > 4 and parts[4] in ("1", "cyclic", "true")
     prec = parts[5] if len(parts) > 5 else "ff"
+    segmented = len(parts) > 6 and parts[6] in ("1", "segmented", "true")
     dev = torch.device("cuda:0")
     w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=SEED, delta=DELTA, flags=0 if cyclic else synth.ZERO_ENDS)
     a, b, c, d = (torch.from_numpy(x).to(dev) for x in w.arrays)
     solve = pbt.solve_cyclic if cyclic else pbt.solve_noncyclic
     with pbt.BtdmaGpuPlan() as plan:
-        plan.create(m, nsys, nrow, nseg, precision=prec, cyclic=cyclic)
+        plan.create(m, nsys, nrow, nseg, precision=prec, cyclic=cyclic, reference_method=segmented)
         t = time_device(plan, (a, b, c), [d], m, nsys, nrow, args.steps, args.warmup, 1, dev, solve)
         plan.status()
     rows = nsys * nrow
     print(json.dumps({"case": {"m": m, "nsys": nsys, "nrow": nrow, "nseg": nseg, "cyclic": cyclic,
-                               "precision": prec}, "ms_per_solve": t / args.steps * 1e3,
+                               "precision": prec, "segmented": segmented}, "ms_per_solve": t / args.steps * 1e3,
                       "block_rows_per_s": rows * args.steps / t,
                       "algorithmic_gbs": rows * bytes_per_row(m) * args.steps / t / 1e9}), flush=True)
 
@@ -985,7 +986,7 @@ def main():
                     help="comma list of extra sections to run beside the headline: variants, mixed, adjoint, "
                          "uneven, shared, lines, cpu; 'all' (default) or 'main' (headline only)")
     ap.add_argument("--case", default="",
-                    help="m,nsys,nrow,nseg[,cyclic][,precision]: time one workload only (profiler captures)")
+                    help="m,nsys,nrow,nseg[,cyclic][,precision][,segmented]: time one workload only (profiler captures)")
     ap.add_argument("--batch-case", default="",
                     help="m,seg_len[,precision]: the uneven batch's systems of block size m only (profiler captures)")
     args = ap.parse_args()

@@ -1436,22 +1436,22 @@ PBT_UNROLL
         }
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
-        // jj = -1: d'; jj < m: column jj of A' (right-hand side A on rows 0,
-        // 1, else -W); jj >= m: column jj - m of C'.  One rolled loop, one
-        // copy of the column solve's code.
+        lu_solve<Num, M>(lu, xd, y);
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
+        st_raw_vec<Num, M>(D + o, opaque(plane0), y);
+        // jj < m: column jj of A' (right-hand side A on rows 0, 1, else -W);
+        // jj >= m: column jj - m of C'.
         {
             const size_t plane = opaque(plane0);
 #pragma unroll 1
-            for (int jj = -1; jj < 2 * M; ++jj) {
+            for (int jj = 0; jj < 2 * M; ++jj) {
                 const bool acol = jj < M;
                 const int j = acol ? jj : jj - M;
                 const size_t co = o + (size_t)(M * j) * plane;
                 Acc v[M];
                 T xj[M];
-                if (jj < 0) {
-PBT_UNROLL
-                    for (int i = 0; i < M; ++i) v[i] = xd[i];
-                } else if (acol && !first2) {
+                if (acol && !first2) {
 PBT_UNROLL
                     for (int i = 0; i < M; ++i) v[i] = Num::acc(Num::neg(Num::lds(slot(kE + i * M + j))));
                 } else {
@@ -1460,21 +1460,12 @@ PBT_UNROLL
                     for (int i = 0; i < M; ++i) v[i] = Num::acc(Num::in(ps + (size_t)i * plane));
                 }
                 lu_solve<Num, M>(lu, v, xj);
-                if (jj < 0) {
+                double* pw = (acol ? AW : CW) + co;
+                const int s0 = acol ? kE + j : j;
 PBT_UNROLL
-                    for (int i = 0; i < M; ++i) {
-                        y[i] = xj[i];
-                        Num::sts(slot(kY + i), xj[i]);
-                    }
-                    st_raw_vec<Num, M>(D + o, plane, y);
-                } else {
-                    double* pw = (acol ? AW : CW) + co;
-                    const int s0 = acol ? kE + j : j;
-PBT_UNROLL
-                    for (int i = 0; i < M; ++i) {
-                        st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
-                        Num::sts(slot(s0 + i * M), xj[i]);
-                    }
+                for (int i = 0; i < M; ++i) {
+                    st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
+                    Num::sts(slot(s0 + i * M), xj[i]);
                 }
                 if (PBT_ROW_FENCE) mem_fence_compiler();
             }
@@ -1606,10 +1597,12 @@ PBT_UNROLL
         }
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, xd, y);
+        st_raw_vec<Num, M>(D, plane, y);
         const size_t ro = rrs * (size_t)(2 * seg);
-        // jj = -1: d'_0; then the A' and C' columns, as in the forward sweep.
+        st_raw_vec<Num, M>(RD + ro, rplane, y);
 #pragma unroll 1
-        for (int jj = -1; jj < 2 * M; ++jj) {
+        for (int jj = 0; jj < 2 * M; ++jj) {
             const bool acol = jj < M;
             const int j = acol ? jj : jj - M;
             double* pw = (acol ? AW : CW) + (size_t)(M * j) * plane;
@@ -1617,20 +1610,14 @@ PBT_UNROLL
             T xj[M];
 PBT_UNROLL
             for (int i = 0; i < M; ++i)
-                v[i] = jj < 0 ? xd[i]
-                              : (acol ? Num::acc(ld_fac<Num>(pw + (size_t)i * plane, raw))
-                                      : Num::acc(Num::neg(Num::lds(slot(j + i * M)))));
+                v[i] = acol ? Num::acc(ld_fac<Num>(pw + (size_t)i * plane, raw))
+                            : Num::acc(Num::neg(Num::lds(slot(j + i * M))));
             lu_solve<Num, M>(lu, v, xj);
-            if (jj < 0) {
-                st_raw_vec<Num, M>(D, plane, xj);
-                st_raw_vec<Num, M>(RD + ro, rplane, xj);
-            } else {
-                double* pr = (acol ? RA : RC) + ro + (size_t)(M * j) * rplane;
+            double* pr = (acol ? RA : RC) + ro + (size_t)(M * j) * rplane;
 PBT_UNROLL
-                for (int i = 0; i < M; ++i) {
-                    st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
-                    Num::sts(pr + (size_t)i * rplane, xj[i]);
-                }
+            for (int i = 0; i < M; ++i) {
+                st_fac<Num>(pw + (size_t)i * plane, xj[i], raw);
+                Num::sts(pr + (size_t)i * rplane, xj[i]);
             }
             if (PBT_ROW_FENCE) mem_fence_compiler();
         }
