@@ -205,6 +205,18 @@ def test_batch_filling_the_gpu_runs_one_segment(cuda, cyclic):
             assert per_system_relerr(m, sub.nsys, nrow, got, ref.D) <= tol
 
 
+def test_one_segment_threshold_is_four_warps_per_sm(cuda):
+    """The switch to one segment per line happens at 4 warps of systems per SM
+    (128 systems per SM): one warp below it the segments are kept."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    m, nrow, nseg = 2, 12, 3
+    for nsys, one_segment in ((128 * sms - 32, False), (128 * sms, True)):
+        w = synth.dominant(m, nsys, nrow, seed=9, delta=1.5)
+        (_, _, _, D3), _ = gpu_solve(w, nseg, precision="ff")
+        (_, _, _, D1), _ = gpu_solve(w, 1, precision="ff")
+        assert np.array_equal(D3, D1) == one_segment
+
+
 def test_plan_mismatch_and_reuse(cuda):
     w = synth.dominant(3, 64, 12, seed=5, delta=2.0)
     a, b, c, d = to_dev(w.arrays, cuda)
