@@ -17,10 +17,10 @@
  * system's own rows.
  *
  * The solve runs, per block size present (largest total cost first), a
- * persistent launch over the local-stage items, one warp per segmented
- * tile for the reduced systems, and a persistent launch over the update
- * items, all on the caller's stream; each launch carries one block size's
- * code.
+ * persistent launch over the local-stage items (the warp that completes a
+ * tile's last segment also solves the tile's reduced system) and a
+ * persistent launch over the update items, on the caller's stream; each
+ * launch carries one block size's code.
  *
  * Tuning (pbt_batch_tuning): the number of segments of each tile is
  * round(N_max / seg_len[m]) (one segment when seg_len[m] <= 0), so long lines
@@ -74,7 +74,7 @@ int pbt_batch_pack(pbt_batch* batch, const double* ua, const double* ub, const d
 int pbt_batch_unpack(pbt_batch* batch, const double* pd, double* ud, void* stream);
 
 /* Solve every system of the batch in place on packed arrays: one memset of
- * the queue state and up to three launches per block size present, no host
+ * the queue state and up to two launches per block size present, no host
  * synchronisation. */
 int pbt_batch_solve(pbt_batch* batch, const double* pa, const double* pb, const double* pc, double* pd,
                     void* stream);

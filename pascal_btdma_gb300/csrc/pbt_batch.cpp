@@ -35,7 +35,7 @@ struct pbt_batch {
     long long* d_user_vec_off = nullptr;
     long long* row_start = nullptr;
     long long pack_total = 0;
-    int* state = nullptr;  // error (always 0), pad, head1[m], head3[m] (kHeads each)
+    int* state = nullptr;  // error (always 0), pad, head1[m], head3[m] (kHeads each), seg_done[ntiles]
     unsigned long long* status = nullptr;
     double *aw = nullptr, *cw = nullptr, *ra = nullptr, *rc = nullptr, *rd = nullptr;
     cudaStream_t last_stream = nullptr;
@@ -47,7 +47,7 @@ namespace {
 constexpr unsigned kBatchMagic = 0x50425442u;
 constexpr int kHeads = PBT_MAX_BLOCK + 1;
 
-size_t state_ints(int) { return (size_t)2 + 2 * kHeads; }
+size_t state_ints(int ntiles) { return (size_t)2 + 2 * kHeads + (size_t)ntiles; }
 
 // One launch of the batch kernel for block size m (pbt_inst.cu instantiates
 // launch_batch per arithmetic and block size).
@@ -386,6 +386,7 @@ int pbt_batch_solve(pbt_batch* b, const double* pa, const double* pb, const doub
     ba.tiles = b->tiles;
     ba.lane_rows = b->lane_rows;
     ba.status = b->status;
+    ba.seg_done = b->state + 2 + 2 * kHeads;
     b->last_grid = 0;
     for (int mm : b->order) {
         ba.items1 = b->items1 + b->off1[mm];

@@ -15,11 +15,15 @@
 //                   nseg = 1 is one item (block Thomas on every lane); a
 //                   tile with nseg = P > 1 gives P items (the modified
 //                   elimination of one segment of every lane), each writing
-//                   its two reduced rows;
-//   k_batch_reduced one warp per segmented tile: the 2P-row reduced system;
+//                   its two reduced rows; the warp that completes a tile's
+//                   last segment solves its 2P-row reduced system;
+//   k_batch_reduced (only with PBT_BATCH_INLINE_REDUCED = 0) one warp per
+//                   segmented tile: the reduced system;
 //   k_batch_update  persistent over the stage-3 items (the interior update of
 //                   one segment of every lane).
-// The kernel boundaries order the stages, so no warp ever waits on another.
+// The kernel boundaries order the stages, so no warp ever waits on another
+// (a tile's reduced system is solved by the warp that finishes it last, found
+// with an atomic counter).
 // Each launch carries one block size's code, with the bodies and register
 // budget k_thomas / k_modi use for that size.
 #pragma once
@@ -43,26 +47,23 @@ __host__ __device__ constexpr int batch_slots() {
     return modi_uses_lu<Num, M>() ? cyclic_slots<Num, M>() : (thomas_uses_lu<M>() ? M * M + M : 0);
 }
 
+// The reduced solves: inside the local-stage launch, by the warp that
+// completes a tile's last segment (PBT_BATCH_INLINE_REDUCED = 1: no warp
+// waits, the other warps go on with their items; cfg 3, segments of 64 rows:
+// float-float 17.94 vs 18.43 ms per sweep, FP64 24.60 vs 25.84 ms), or as a
+// launch of their own, one warp per segmented tile (0).
+#ifndef PBT_BATCH_INLINE_REDUCED
+#define PBT_BATCH_INLINE_REDUCED 1
+#endif
+
 template <class Num, int M>
-__device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTile& tl, int t, int seg, unsigned& bad) {
-    const int lane = threadIdx.x & 31;
-    const size_t plane = (size_t)32 * tl.rows, rs = 32;
-    const int n_lane = tl.rows;  // every system of the tile is padded to its rows
-    if (lane >= tl.lanes) return;  // the lane rejoins at the next claim
-    const size_t mo = (size_t)tl.mat_off + lane, vo = (size_t)tl.vec_off + lane;
+__device__ __forceinline__ void batch_modi(const BatchArgs& ba, const BatchTile& tl, int seg, int lane, size_t plane,
+                                           size_t rplane, unsigned& bad) {
     extern __shared__ double batch_cps[];
-    if (seg < 0) {
-        if constexpr (thomas_uses_lu<M>()) {
-            thomas_body_lu<Num, M>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo, batch_cps + threadIdx.x,
-                                   blockDim.x, plane, rs, n_lane, true, bad);
-        } else {
-            thomas_body<Num, M>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo, plane, rs, n_lane, true, bad);
-        }
-        return;
-    }
-    const size_t rplane = (size_t)32 * 2 * tl.nseg;
+    const size_t rs = 32;
+    const size_t mo = (size_t)tl.mat_off + lane, vo = (size_t)tl.vec_off + lane;
     int f, l;
-    seg_rows(n_lane, tl.nseg, seg, f, l);
+    seg_rows(tl.rows, tl.nseg, seg, f, l);
     const size_t fo = (size_t)f * rs;
     if constexpr (modi_uses_lu<Num, M>()) {
         modi_body_lu<Num, M>(ba.a + mo + fo, ba.b + mo + fo, ba.c + mo + fo, ba.d + vo + fo, ba.aw + mo + fo,
@@ -75,6 +76,47 @@ __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTil
                           ba.rc + tl.red_mat_off + lane, ba.rd + tl.red_vec_off + lane, rplane, rs, seg, bad);
     }
 }
+
+template <class Num, int M>
+__device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTile& tl, int t, int seg, unsigned& bad) {
+    const int lane = threadIdx.x & 31;
+    const size_t plane = (size_t)32 * tl.rows, rs = 32;
+    const int n_lane = tl.rows;  // every system of the tile is padded to its rows
+    const bool active = lane < tl.lanes;
+    const size_t mo = (size_t)tl.mat_off + lane, vo = (size_t)tl.vec_off + lane;
+    extern __shared__ double batch_cps[];
+    if (seg < 0) {
+        if (!active) return;  // the lane rejoins at the next claim
+        if constexpr (thomas_uses_lu<M>()) {
+            // d solved apart: in this kernel, beside the local stage's
+            // body, the merged column loop raises the spills (cfg 3:
+            // float-float 17.90 vs 18.43 ms per sweep).
+            thomas_body_lu<Num, M, false>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo,
+                                          batch_cps + threadIdx.x, blockDim.x, plane, rs, n_lane, true, bad);
+        } else {
+            thomas_body<Num, M>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo, plane, rs, n_lane, true, bad);
+        }
+        return;
+    }
+    const size_t rplane = (size_t)32 * 2 * tl.nseg;
+    if (active) batch_modi<Num, M>(ba, tl, seg, lane, plane, rplane, bad);
+    if constexpr (PBT_BATCH_INLINE_REDUCED) {
+        // Publish this segment; the warp completing the tile solves its
+        // reduced system (no warp waits: the update is the next launch).
+        __threadfence();
+        __syncwarp();
+        int done = 0;
+        if (lane == 0) done = atomicAdd(&ba.seg_done[t], 1);
+        done = __shfl_sync(0xffffffffu, done, 0);
+        if (done == tl.nseg - 1) {
+            __threadfence();
+            if (active)
+                reduced_body<Num, M>(ba.ra + tl.red_mat_off + lane, ba.rc + tl.red_mat_off + lane,
+                                     ba.rd + tl.red_vec_off + lane, rplane, rs, 2 * tl.nseg, bad);
+        }
+    }
+}
+
 
 // Registers of the local stage: the split bodies (m = 5, 6 in FP64 and
 // float-float) are built for 128 registers (4 CTAs of 128 threads an SM);
@@ -158,7 +200,7 @@ cudaError_t launch_batch(const BatchArgs& ba, int warps, cudaStream_t s, int* gr
         const int grid = sms * (per_sm > 0 ? per_sm : 1);
         if (grid_out) *grid_out = grid;
         if (ba.n1 > 0) k_batch_local<Num, M><<<grid, 32 * warps, smem, s>>>(ba);
-        if (ba.n_red > 0) k_batch_reduced<Num, M><<<(ba.n_red + 3) / 4, 128, 0, s>>>(ba);
+        if (!PBT_BATCH_INLINE_REDUCED && ba.n_red > 0) k_batch_reduced<Num, M><<<(ba.n_red + 3) / 4, 128, 0, s>>>(ba);
         if (ba.n3 > 0) {
             int per_sm3 = 0;
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm3, k_batch_update<Num, M>, 128, 0);

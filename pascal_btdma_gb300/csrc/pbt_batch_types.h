@@ -35,6 +35,7 @@ struct BatchArgs {
     int n1, n3, n_red;
     int* head1;            // queue heads, zeroed before every solve
     int* head3;
+    int* seg_done;         // per tile: segments done (zeroed before every solve)
     unsigned long long* status;  // zero pivots, range flag
 };
 

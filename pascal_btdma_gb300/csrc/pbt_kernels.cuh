@@ -533,7 +533,7 @@ __host__ __device__ constexpr bool thomas_uses_lu() {
 // m*m extra FP64 adds in the FP64 solve).  The operations and their order are
 // exactly those of the TMA-staged kernel k_thomas_staged, so the two agree
 // bit for bit.
-template <class Num, int M>
+template <class Num, int M, bool MergeY = (PBT_LU_MERGE_Y != 0)>
 __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B, const double* C, double* D,
                                                double* CW, double* cps, int cstride, size_t plane0, size_t rs,
                                                int N, bool raw, unsigned& bad) {
@@ -611,10 +611,9 @@ PBT_UNROLL
         }
         LU<Num, M> lu;
         lu_factor<Num, M>(r, lu, bad);
-#if PBT_LU_MERGE_Y
-        // y as column -1 of the rolled column loop (one copy of the column
-        // solve's code for y and C).
-        if constexpr (lu_rolled<Num>()) {
+        // MergeY: y as column -1 of the rolled column loop (one copy of the
+        // column solve's code for y and C).
+        if constexpr (MergeY && lu_rolled<Num>()) {
             const size_t plane = opaque(plane0);
             const double* pc = C + o;
             double* pw = CW + o;
@@ -675,7 +674,6 @@ PBT_UNROLL
             st_raw_vec<Num, M>(D + o, plane, y);
             continue;
         }
-#endif
         lu_solve<Num, M>(lu, xd, y);
         if constexpr (lu_rolled<Num>()) {
 PBT_UNROLL
