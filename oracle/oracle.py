@@ -85,6 +85,16 @@ def solve_noncyclic_cpu(m, nsys, nrow, nseg, A, B, Cm, D, nthreads=0) -> int:
                   "solve_noncyclic_cpu")
 
 
+def solve_cyclic_cpu(m, nsys, nrow, nseg, A, B, Cm, D, nthreads=0) -> int:
+    return _check(lib().pbto_solve_cyclic_cpu(m, nsys, nrow, nseg, _p(A), _p(B), _p(Cm), _p(D), nthreads),
+                  "solve_cyclic_cpu")
+
+
+def block_thomas_cyclic_cpu(m, nsys, nrow, A, B, Cm, D, nthreads=0) -> int:
+    return _check(lib().pbto_block_thomas_cyclic_cpu(m, nsys, nrow, _p(A), _p(B), _p(Cm), _p(D), nthreads),
+                  "block_thomas_cyclic_cpu")
+
+
 def gpu_to_cpu(m, nsys, nrow, is_matrix, g: np.ndarray) -> np.ndarray:
     out = np.empty_like(g)
     lib().pbto_gpu_to_cpu(m, nsys, nrow, int(is_matrix), _p(g), _p(out))

@@ -27,7 +27,7 @@ def run(w, arrays, nseg, **kw):
 @pytest.mark.parametrize("m,nsys,nrow,nseg,kw", [
     (3, 100, 40, 1, {}), (5, 70, 24, 1, {"precision": "ff"}), (4, 33, 48, 4, {}), (2, 64, 30, 3, {"precision": "ff"}),
     (10, 7, 12, 1, {}), (5, 64, 64, 1, {"precision": "fp32_refine", "tol": 1e-12}),
-    (4, 40, 32, 4, {"cyclic": True}),
+    (4, 40, 32, 4, {"cyclic": True}), (5, 40, 24, 1, {"cyclic": True, "precision": "ff"}),
 ])
 def test_cpu_layout_equals_gpu_layout(cuda, m, nsys, nrow, nseg, kw):
     flags = 0 if kw.get("cyclic") else synth.ZERO_ENDS
@@ -38,12 +38,16 @@ def test_cpu_layout_equals_gpu_layout(cuda, m, nsys, nrow, nseg, kw):
     assert np.array_equal(out_cpu[3], O.gpu_to_cpu(m, nsys, nrow, False, out_gpu[3]))
     for k in range(3):
         assert np.array_equal(out_cpu[k], cpu[k])  # A, B, C untouched
+    ref = [x.copy() for x in cpu]
     if not kw.get("cyclic"):
-        ref = [x.copy() for x in cpu]
         O.solve_noncyclic_cpu(m, nsys, nrow, nseg, *ref)
-        ref_g = O.cpu_to_gpu(m, nsys, nrow, False, ref[3])
-        tol = 1e-10 if kw.get("precision") == "fp32_refine" else 1e-12
-        assert per_system_relerr(m, nsys, nrow, out_gpu[3], ref_g) <= tol
+    elif nseg == 1:
+        O.block_thomas_cyclic_cpu(m, nsys, nrow, *ref)
+    else:
+        O.solve_cyclic_cpu(m, nsys, nrow, nseg, *ref)
+    ref_g = O.cpu_to_gpu(m, nsys, nrow, False, ref[3])
+    tol = 1e-10 if kw.get("precision") == "fp32_refine" else 1e-12
+    assert per_system_relerr(m, nsys, nrow, out_gpu[3], ref_g) <= tol
 
 
 def test_cpu_layout_profiled_total_covers_conversion(cuda):

@@ -103,7 +103,7 @@ def test_whole_line_cyclic_matches_dense_solve(m, nsys, nrow):
         assert np.abs(xo - x).max() <= 1e-12 * np.abs(x).max()
     # The CPU-layout entry gives the same bits.
     c = [O.gpu_to_cpu(m, nsys, nrow, i < 3, v) for i, v in enumerate(w.arrays)]
-    assert O.lib().pbto_block_thomas_cyclic_cpu(m, nsys, nrow, *[O._p(v) for v in c], 0) == 0
+    assert O.block_thomas_cyclic_cpu(m, nsys, nrow, *c) == 0
     assert np.array_equal(O.cpu_to_gpu(m, nsys, nrow, False, c[3]), got.D)
 
 
