@@ -110,9 +110,16 @@ __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTil
         done = __shfl_sync(0xffffffffu, done, 0);
         if (done == tl.nseg - 1) {
             __threadfence();
-            if (active)
-                reduced_body<Num, M>(ba.ra + tl.red_mat_off + lane, ba.rc + tl.red_mat_off + lane,
-                                     ba.rd + tl.red_vec_off + lane, rplane, rs, 2 * tl.nseg, bad);
+            if (active) {
+                if constexpr (modi_uses_lu<Num, M>()) {
+                    reduced_body_lu<Num, M>(ba.ra + tl.red_mat_off + lane, ba.rc + tl.red_mat_off + lane,
+                                            ba.rd + tl.red_vec_off + lane, batch_cps + threadIdx.x, blockDim.x,
+                                            rplane, rs, 2 * tl.nseg, bad);
+                } else {
+                    reduced_body<Num, M>(ba.ra + tl.red_mat_off + lane, ba.rc + tl.red_mat_off + lane,
+                                         ba.rd + tl.red_vec_off + lane, rplane, rs, 2 * tl.nseg, bad);
+                }
+            }
         }
     }
 }

@@ -1741,6 +1741,112 @@ PBT_UNROLL
     bad |= range_bits<Num>(amax, true);
 }
 
+// The reduced solve with the row step split (lu_factor / lu_solve), for the
+// batch's local-stage launch at m = 5, 6, where the fused reduced_body would
+// spill heavily at that launch's 128 registers.  Same recurrence and stores as
+// reduced_body (B = I; C' overwrites rc, the solution rd, both raw); C'_{q-1}
+// and y_{q-1} live in this thread's shared-memory slots (k*M + j and
+// M*M + k), as in thomas_body_lu.
+template <class Num, int M>
+__device__ __forceinline__ void reduced_body_lu(const double* RA, double* RC, double* RD, double* cps, int cstride,
+                                                size_t plane0, size_t rs, int R, unsigned& bad) {
+    using T = typename Num::T;
+    using Acc = typename Num::Acc;
+    constexpr int kY = M * M;
+    auto slot = [&](int s) -> double* { return cps + s * cstride; };
+    T y[M];
+    {
+        // Row 0: B = I, so [C'|y] = [C|d] exactly.
+        const size_t plane = opaque(plane0);
+PBT_UNROLL
+        for (int j = 0; j < M; ++j)
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) Num::sts(slot(i * M + j), Num::lds(RC + (size_t)(i + M * j) * plane));
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            y[i] = Num::lds(RD + (size_t)i * plane);
+            Num::sts(slot(kY + i), y[i]);
+        }
+    }
+    for (int q = 1; q < R; ++q) {
+        const size_t o = (size_t)q * rs;
+        const bool last = (q == R - 1);
+        Acc r[M][M], xd[M];
+        {
+            const size_t plane = opaque(plane0);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                xd[i] = Num::acc(Num::lds(RD + o + (size_t)i * plane));
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) r[i][j] = Num::acc(i == j ? Num::one() : Num::zero());
+            }
+            const double* pa = RA + o;
+#pragma unroll 1
+            for (int k = 0; k < M; ++k) {
+                T ck[M], ak[M];
+PBT_UNROLL
+                for (int j = 0; j < M; ++j) ck[j] = Num::lds(slot(k * M + j));
+                const T yk = Num::lds(slot(kY + k));
+PBT_UNROLL
+                for (int i = 0; i < M; ++i, pa += plane) ak[i] = Num::lds(pa);
+PBT_UNROLL
+                for (int i = 0; i < M; ++i) {
+PBT_UNROLL
+                    for (int j = 0; j < M; ++j) Num::msub(r[i][j], ak[i], ck[j]);
+                    Num::msub(xd[i], ak[i], yk);
+                }
+                if (PBT_ROW_FENCE) mem_fence_compiler();
+            }
+        }
+        LU<Num, M> lu;
+        lu_factor<Num, M>(r, lu, bad);
+        lu_solve<Num, M>(lu, xd, y);
+        const size_t plane = opaque(plane0);
+        st_raw_vec<Num, M>(RD + o, plane, y);
+        if (last) break;
+PBT_UNROLL
+        for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
+#pragma unroll 1
+        for (int j = 0; j < M; ++j) {
+            double* pc = RC + o + (size_t)(M * j) * plane;
+            Acc cj[M];
+            T xj[M];
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) cj[i] = Num::acc(Num::lds(pc + (size_t)i * plane));
+            lu_solve<Num, M>(lu, cj, xj);
+PBT_UNROLL
+            for (int i = 0; i < M; ++i) {
+                Num::sts(pc + (size_t)i * plane, xj[i]);
+                Num::sts(slot(i * M + j), xj[i]);
+            }
+            if (PBT_ROW_FENCE) mem_fence_compiler();
+        }
+    }
+    // Backward, as reduced_body, with its range check of the line.
+    unsigned amax = 0;
+PBT_UNROLL
+    for (int i = 0; i < M; ++i) amax = max(amax, Num::mag(y[i]));
+    for (int q = R - 2; q >= 0; --q) {
+        const size_t o = (size_t)q * rs;
+        const size_t plane = opaque(plane0);
+        T c[M][M], t[M];
+        ld_raw_blk<Num, M>(c, RC + o, plane);
+        ld_raw_vec<Num, M>(t, RD + o, plane);
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) {
+            Acc s = Num::acc(t[i]);
+PBT_UNROLL
+            for (int k = 0; k < M; ++k) Num::msub(s, c[i][k], y[k]);
+            t[i] = Num::fin(s);
+            amax = max(amax, Num::mag(t[i]));
+        }
+PBT_UNROLL
+        for (int i = 0; i < M; ++i) y[i] = t[i];
+        st_raw_vec<Num, M>(RD + o, plane, y);
+    }
+    bad |= range_bits<Num>(amax, true);
+}
+
 template <class Num, int M>
 __global__ void __launch_bounds__(128) k_reduced(const SolveArgs g) {
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
