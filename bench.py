@@ -680,7 +680,9 @@ def run_ours(args):
         vsolve = pbt.solve_cyclic if vcyc else solve
         va, vb, vc, vd = (torch.from_numpy(x).to(dev) for x in vw.arrays)
         vrows = vns * vn
+        fills = vns >= 128 * torch.cuda.get_device_properties(dev).multi_processor_count
         entry = {"m": vm, "nsys": vns, "nrow": vn, "nseg": vp, "cyclic": vcyc,
+                 "default_plan_solves_as": (f"{vp} segments" if vp > 1 and not fills else "one segment per line"),
                  "l2": "flushed before each solve" if vrows * bytes_per_row(vm) < L2_FIT_BYTES else "inputs > L2"}
         xs = {}
         # With nseg > 1 a batch that fills the GPU is solved one segment per
@@ -729,7 +731,10 @@ def run_ours(args):
         ma, mb, mc, md = (torch.from_numpy(x).to(dev) for x in mw.arrays)
         mrows = NSYS * NROW
         for nseg_m in segs:
-            entry = {"delta": delta, "nseg": nseg_m, "row_scale": "log-uniform [1e-3, 1e3]"}
+            fills = NSYS >= 128 * torch.cuda.get_device_properties(dev).multi_processor_count
+            entry = {"delta": delta, "nseg": nseg_m, "row_scale": "log-uniform [1e-3, 1e3]",
+                     "default_plan_solves_as": (f"{nseg_m} segments" if nseg_m > 1 and not fills
+                                                else "one segment per line")}
             ref = md.clone()
             with pbt.BtdmaGpuPlan() as p64:
                 p64.create(M, NSYS, NROW, nseg_m, precision="fp64")
