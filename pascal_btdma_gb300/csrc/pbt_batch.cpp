@@ -20,7 +20,6 @@ struct pbt_batch {
     // items3; one persistent launch per block size present, in `order`.
     int off1[PBT_MAX_BLOCK + 1] = {}, cnt1[PBT_MAX_BLOCK + 1] = {};
     int off3[PBT_MAX_BLOCK + 1] = {}, cnt3[PBT_MAX_BLOCK + 1] = {};
-    int offr[PBT_MAX_BLOCK + 1] = {}, cntr[PBT_MAX_BLOCK + 1] = {};
     std::vector<int> order;
     std::vector<long long> user_mat_off, user_vec_off;
     long long user_mat = 0, user_vec = 0, packed_mat = 0, packed_vec = 0, red_mat = 0, red_vec = 0;
@@ -30,7 +29,6 @@ struct pbt_batch {
     int* sys_of = nullptr;
     int2* items1 = nullptr;
     int2* items3 = nullptr;
-    int* red_tiles = nullptr;
     long long* d_user_mat_off = nullptr;
     long long* d_user_vec_off = nullptr;
     long long* row_start = nullptr;
@@ -100,7 +98,6 @@ int dalloc(double** p, long long n) {
 }
 
 void free_batch(pbt_batch* b) {
-    cudaFree(b->red_tiles);
     cudaFree(b->tiles);
     cudaFree(b->lane_rows);
     cudaFree(b->sys_of);
@@ -232,7 +229,6 @@ int pbt_batch_create(pbt_batch** out, int nsys, const int* m, const int* nrow, i
         double cost;
     };
     std::vector<int2> items1, items3;
-    std::vector<int> red_tiles;
     std::vector<char> seen(b->ntiles, 0);
     std::vector<std::pair<double, int>> by_cost;
     for (int mm = 1; mm <= PBT_BATCH_MAX_BLOCK; ++mm) {
@@ -262,13 +258,6 @@ int pbt_batch_create(pbt_batch** out, int nsys, const int* m, const int* nrow, i
         }
         b->cnt1[mm] = (int)items1.size() - b->off1[mm];
         b->cnt3[mm] = (int)items3.size() - b->off3[mm];
-        // Reduced solves, longest first.
-        b->offr[mm] = (int)red_tiles.size();
-        for (int t = 0; t < b->ntiles; ++t)
-            if (tiles[t].m == mm && tiles[t].nseg > 1) red_tiles.push_back(t);
-        std::stable_sort(red_tiles.begin() + b->offr[mm], red_tiles.end(),
-                         [&](int x, int y) { return tiles[x].nseg > tiles[y].nseg; });
-        b->cntr[mm] = (int)red_tiles.size() - b->offr[mm];
         by_cost.push_back({total, mm});
     }
     std::stable_sort(by_cost.begin(), by_cost.end(), [](const std::pair<double, int>& x, const std::pair<double, int>& y) {
@@ -279,7 +268,7 @@ int pbt_batch_create(pbt_batch** out, int nsys, const int* m, const int* nrow, i
     b->n3 = (int)items3.size();
     int rc = PBT_OK;
     if ((rc = upload(&b->tiles, tiles)) || (rc = upload(&b->lane_rows, lane_rows)) || (rc = upload(&b->sys_of, sys_of)) ||
-        (rc = upload(&b->items1, items1)) || (rc = upload(&b->items3, items3)) || (rc = upload(&b->red_tiles, red_tiles)) ||
+        (rc = upload(&b->items1, items1)) || (rc = upload(&b->items3, items3)) ||
         (rc = upload(&b->d_user_mat_off, b->user_mat_off)) || (rc = upload(&b->d_user_vec_off, b->user_vec_off)) ||
         (rc = upload(&b->row_start, row_start)))
         goto fail_out;
@@ -391,10 +380,8 @@ int pbt_batch_solve(pbt_batch* b, const double* pa, const double* pb, const doub
     for (int mm : b->order) {
         ba.items1 = b->items1 + b->off1[mm];
         ba.items3 = b->items3 + b->off3[mm];
-        ba.red_tiles = b->red_tiles + b->offr[mm];
         ba.n1 = b->cnt1[mm];
         ba.n3 = b->cnt3[mm];
-        ba.n_red = b->cntr[mm];
         ba.head1 = b->state + 2 + mm;
         ba.head3 = b->state + 2 + kHeads + mm;
         int grid = 0;

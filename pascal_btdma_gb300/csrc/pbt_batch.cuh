@@ -17,8 +17,6 @@
 //                   elimination of one segment of every lane), each writing
 //                   its two reduced rows; the warp that completes a tile's
 //                   last segment solves its 2P-row reduced system;
-//   k_batch_reduced (only with PBT_BATCH_INLINE_REDUCED = 0) one warp per
-//                   segmented tile: the reduced system;
 //   k_batch_update  persistent over the stage-3 items (the interior update of
 //                   one segment of every lane).
 // The kernel boundaries order the stages, so no warp ever waits on another
@@ -47,14 +45,6 @@ __host__ __device__ constexpr int batch_slots() {
     return modi_uses_lu<Num, M>() ? cyclic_slots<Num, M>() : (thomas_uses_lu<M>() ? M * M + M : 0);
 }
 
-// The reduced solves: inside the local-stage launch, by the warp that
-// completes a tile's last segment (PBT_BATCH_INLINE_REDUCED = 1: no warp
-// waits, the other warps go on with their items; cfg 3, segments of 64 rows:
-// float-float 17.94 vs 18.43 ms per sweep, FP64 24.60 vs 25.84 ms), or as a
-// launch of their own, one warp per segmented tile (0).
-#ifndef PBT_BATCH_INLINE_REDUCED
-#define PBT_BATCH_INLINE_REDUCED 1
-#endif
 
 template <class Num, int M>
 __device__ __forceinline__ void batch_modi(const BatchArgs& ba, const BatchTile& tl, int seg, int lane, size_t plane,
@@ -100,9 +90,13 @@ __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTil
     }
     const size_t rplane = (size_t)32 * 2 * tl.nseg;
     if (active) batch_modi<Num, M>(ba, tl, seg, lane, plane, rplane, bad);
-    if constexpr (PBT_BATCH_INLINE_REDUCED) {
+    {
         // Publish this segment; the warp completing the tile solves its
-        // reduced system (no warp waits: the update is the next launch).
+        // reduced system while the other warps go on with their items (no
+        // warp waits: the update is the next launch).  Measured against a
+        // launch of its own, one warp per segmented tile (cfg 3, segments of
+        // 64 rows): float-float 17.94 vs 18.43 ms per sweep, FP64 24.60 vs
+        // 25.84 ms.
         __threadfence();
         __syncwarp();
         int done = 0;
@@ -143,21 +137,6 @@ __global__ void __launch_bounds__(128, batch_min_ctas<Num, M>()) k_batch_local(c
         const BatchTile tl = ba.tiles[it.x];
         batch_stage1<Num, M>(ba, tl, it.x, it.y, bad);
     }
-    report_status(ba.status, bad);
-}
-
-// One warp per segmented tile of this block size.
-template <class Num, int M>
-__global__ void __launch_bounds__(128) k_batch_reduced(const BatchArgs ba) {
-    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (w >= ba.n_red) return;
-    const int t = ba.red_tiles[w];
-    const BatchTile tl = ba.tiles[t];
-    const int lane = threadIdx.x & 31;
-    if (lane >= tl.lanes) return;
-    unsigned bad = 0;
-    reduced_body<Num, M>(ba.ra + tl.red_mat_off + lane, ba.rc + tl.red_mat_off + lane, ba.rd + tl.red_vec_off + lane,
-                         (size_t)32 * 2 * tl.nseg, 32, 2 * tl.nseg, bad);
     report_status(ba.status, bad);
 }
 
@@ -207,7 +186,6 @@ cudaError_t launch_batch(const BatchArgs& ba, int warps, cudaStream_t s, int* gr
         const int grid = sms * (per_sm > 0 ? per_sm : 1);
         if (grid_out) *grid_out = grid;
         if (ba.n1 > 0) k_batch_local<Num, M><<<grid, 32 * warps, smem, s>>>(ba);
-        if (!PBT_BATCH_INLINE_REDUCED && ba.n_red > 0) k_batch_reduced<Num, M><<<(ba.n_red + 3) / 4, 128, 0, s>>>(ba);
         if (ba.n3 > 0) {
             int per_sm3 = 0;
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm3, k_batch_update<Num, M>, 128, 0);

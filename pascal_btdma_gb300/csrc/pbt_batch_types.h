@@ -31,8 +31,7 @@ struct BatchArgs {
     const int* lane_rows;  // [tile*32 + lane]: N of that system, 0 for an empty lane
     const int2* items1;    // (tile, segment or -1 for a whole-line Thomas item)
     const int2* items3;    // (tile, segment)
-    const int* red_tiles;  // the segmented tiles
-    int n1, n3, n_red;
+    int n1, n3;
     int* head1;            // queue heads, zeroed before every solve
     int* head3;
     int* seg_done;         // per tile: segments done (zeroed before every solve)
