@@ -495,6 +495,8 @@ pbt::SolveArgs make_args(pbt_plan* p, double* a, double* b, double* c, double* d
     g.nseg = p->desc.nseg;
     g.tpb = pick_tpb(p, work_items);
     g.stream = s;
+    g.sms = p->sms;
+    g.tpb_auto = p->desc.threads_per_block == 0;
     return g;
 }
 

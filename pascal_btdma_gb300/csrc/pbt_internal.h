@@ -33,6 +33,8 @@ struct SolveArgs {
     int nseg;
     int tpb;  // threads per block
     cudaStream_t stream;
+    int sms = 0;       // SMs of the device (0: unknown)
+    int tpb_auto = 0;  // 1: the CTA size is the library's choice (kernels may pick their own)
 };
 
 // Strided lines (pbt_solve_noncyclic_lines): line sys at

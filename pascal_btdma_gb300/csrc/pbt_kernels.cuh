@@ -517,6 +517,34 @@ __host__ __device__ constexpr bool lu_ldg() {
 }
 constexpr int kThomasLuMinBlock = PBT_THOMAS_LU_MIN;
 constexpr int kThomasLuMaxBlock = 6;
+// Whether the split-row-step kernels keep their CTA's warps in step row by
+// row (a barrier per row; InStep of thomas_body_lu / modi_body_lu).  Measured
+// on GB300 (m = 5): float-float issue is bound by instruction fetch, and
+// warps that run the same rows together share the instruction cache -- the
+// pencil batch (65536 x 256) 5.93 -> 5.37 ms in one segment, 18.7 -> 12.9 ms
+// in 16 (256-thread CTAs); the FP64 solve is bound by its pipe and gains
+// nothing (12.65 ms without, 14.09 ms with).
+template <class Num>
+__host__ __device__ constexpr bool rows_in_step() {
+    return std::is_same<Num, FF>::value;
+}
+
+// CTA size of the in-step kernels: up to 256 threads, as many as two CTAs an
+// SM allow with `smem_thread` bytes of shared memory a thread, reduced so
+// that `units` threads make whole waves of CTAs over the SMs (65536 systems
+// on 152 SMs: 224 threads, 293 CTAs, at most two an SM).  A CTA size fixed by
+// the caller (threads_per_block) is kept.
+inline int in_step_tpb(const SolveArgs& g, long long units, size_t smem_thread) {
+    if (!g.tpb_auto) return g.tpb;
+    int cap = 256;
+    while (cap > 32 && 2 * ((size_t)cap * smem_thread + 1024) > 228u * 1024u) cap -= 32;
+    const long long sms = g.sms > 0 ? g.sms : 1;
+    const long long waves = (units + cap * sms - 1) / (cap * sms);
+    long long tpb = (units + waves * sms - 1) / (waves * sms);
+    tpb = (tpb + 31) / 32 * 32;
+    return (int)(tpb < 32 ? 32 : (tpb > cap ? cap : tpb));
+}
+
 template <int M>
 __host__ __device__ constexpr bool thomas_uses_lu() {
     return M >= kThomasLuMinBlock && M <= kThomasLuMaxBlock;
@@ -533,7 +561,12 @@ __host__ __device__ constexpr bool thomas_uses_lu() {
 // m*m extra FP64 adds in the FP64 solve).  The operations and their order are
 // exactly those of the TMA-staged kernel k_thomas_staged, so the two agree
 // bit for bit.
-template <class Num, int M, bool MergeY = (PBT_LU_MERGE_Y != 0)>
+//
+// InStep: the CTA's threads meet at a barrier at the top of every row (forward
+// and backward), so its warps run the same stretch of code together and share
+// the instruction cache; a thread without a system (past the last one, in a
+// partial CTA) takes the same barriers in thomas_idle_rows.
+template <class Num, int M, bool MergeY = (PBT_LU_MERGE_Y != 0), bool InStep = false>
 __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B, const double* C, double* D,
                                                double* CW, double* cps, int cstride, size_t plane0, size_t rs,
                                                int N, bool raw, unsigned& bad) {
@@ -546,6 +579,7 @@ __device__ __forceinline__ void thomas_body_lu(const double* A, const double* B,
     T y[M];
     unsigned amax = 0;
     for (int q = 0; q < N; ++q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const bool last = (q == N - 1);
         Acc r[M][M], xd[M];
@@ -736,6 +770,7 @@ PBT_UNROLL
         }
     }
     for (int q = N - 2; q >= 0; --q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         T c[M][M], t[M];
@@ -756,16 +791,27 @@ PBT_UNROLL
 }
 
 
+// The barriers of thomas_body_lu<..., InStep = true> for a thread without a
+// system: the same loop headers, one barrier per forward and backward row.
+__device__ __forceinline__ void thomas_idle_rows(int N) {
+    for (int q = 0; q < N; ++q) cta_row_barrier();
+    for (int q = N - 2; q >= 0; --q) cta_row_barrier();
+}
+
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
+    constexpr bool kStep = thomas_uses_lu<M>() && rows_in_step<Num>();
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
+    if (sys >= g.nsys) {
+        if constexpr (kStep) thomas_idle_rows(g.nrow);
+        return;
+    }
     unsigned bad = 0;
     if constexpr (thomas_uses_lu<M>()) {
         extern __shared__ double thomas_cps[];
-        thomas_body_lu<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, thomas_cps + threadIdx.x,
-                               blockDim.x, (size_t)g.nsys * g.nrow, (size_t)g.nsys, g.nrow, g.factors_raw != 0,
-                               bad);
+        thomas_body_lu<Num, M, (PBT_LU_MERGE_Y != 0), kStep>(
+            g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, thomas_cps + threadIdx.x, blockDim.x,
+            (size_t)g.nsys * g.nrow, (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
     } else {
         thomas_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
                             (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
@@ -1343,7 +1389,7 @@ __host__ __device__ constexpr bool modi_uses_lu() {
     return M >= PBT_MODI_LU_MIN && M <= 6 && !std::is_same<Num, F32>::value;
 }
 
-template <class Num, int M>
+template <class Num, int M, bool InStep = false>
 __device__ __forceinline__ void modi_body_lu(const double* A, const double* B, const double* C, double* D,
                                              double* AW, double* CW, double* cps, int cstride, size_t plane0,
                                              size_t rs, int n, bool raw, double* RA, double* RC, double* RD,
@@ -1359,6 +1405,7 @@ __device__ __forceinline__ void modi_body_lu(const double* A, const double* B, c
     // Forward.  Rows 0, 1: [A'|C'|d'] = B^{-1}[A|C|d]; rows 2..n-1:
     // R = B - A C'_{q-1}; [A'|C'|d'] = R^{-1}[-A A'_{q-1} | C | d - A d'_{q-1}].
     for (int q = 0; q < n; ++q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const bool first2 = (q < 2);
         if (!first2) {
@@ -1498,6 +1545,7 @@ PBT_UNROLL
         ld_raw_vec<Num, M>(y, D + o1, plane);
     }
     for (int q = n - 3; q >= 1; --q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         T c[M][M], t[M];
@@ -1622,20 +1670,32 @@ PBT_UNROLL
     }
 }
 
+// The barriers of modi_body_lu<..., InStep = true> for a thread without a
+// system: the same loop headers, one barrier per forward and backward row.
+__device__ __forceinline__ void modi_idle_rows(int n) {
+    for (int q = 0; q < n; ++q) cta_row_barrier();
+    for (int q = n - 3; q >= 1; --q) cta_row_barrier();
+}
+
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_modi_lu(const SolveArgs g) {
+    constexpr bool kStep = rows_in_step<Num>();
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
-    extern __shared__ double thomas_cps[];
     const int seg = blockIdx.y;
     int f, l;
     seg_rows(g.nrow, g.nseg, seg, f, l);
+    if (sys >= g.nsys) {
+        if constexpr (kStep) modi_idle_rows(l - f + 1);
+        return;
+    }
+    extern __shared__ double thomas_cps[];
     const size_t rs = (size_t)g.nsys;
     const size_t fo = (size_t)f * rs + sys;
     unsigned bad = 0;
-    modi_body_lu<Num, M>(g.a + fo, g.b + fo, g.c + fo, g.d + fo, g.aw + fo, g.cw + fo, thomas_cps + threadIdx.x,
-                         blockDim.x, rs * g.nrow, rs, l - f + 1, g.factors_raw != 0, g.ra + sys, g.rc + sys,
-                         g.rd + sys, rs * 2 * g.nseg, rs, seg, bad);
+    modi_body_lu<Num, M, kStep>(g.a + fo, g.b + fo, g.c + fo, g.d + fo, g.aw + fo, g.cw + fo,
+                                thomas_cps + threadIdx.x, blockDim.x, rs * g.nrow, rs, l - f + 1,
+                                g.factors_raw != 0, g.ra + sys, g.rc + sys, g.rd + sys, rs * 2 * g.nseg, rs, seg,
+                                bad);
     report_status(g.status, bad);
 }
 
@@ -2516,8 +2576,15 @@ inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) /
 
 template <class Num, int M>
 cudaError_t launch_thomas(const SolveArgs& g) {
-    const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
-    const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * (M * M + M) * sizeof(double) : 0;
+    constexpr bool kStep = thomas_uses_lu<M>() && rows_in_step<Num>();
+    constexpr size_t kSmemThread = thomas_uses_lu<M>() ? (M * M + M) * sizeof(double) : 0;
+    const int tpb = kStep ? in_step_tpb(g, g.nsys, kSmemThread) : (g.tpb < kThomasThreads ? g.tpb : kThomasThreads);
+    const size_t smem = (size_t)tpb * kSmemThread;
+    if (smem > 48u * 1024u) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_thomas<Num, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     k_thomas<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g);
     return cudaGetLastError();
 }
@@ -2554,8 +2621,15 @@ cudaError_t launch_thomas_cyclic(const SolveArgs& g) {
 template <class Num, int M>
 cudaError_t launch_modi(const SolveArgs& g) {
     if constexpr (modi_uses_lu<Num, M>()) {
-        const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
-        const size_t smem = (size_t)tpb * cyclic_slots<Num, M>() * sizeof(double);
+        constexpr size_t kSmemThread = cyclic_slots<Num, M>() * sizeof(double);
+        const int tpb = rows_in_step<Num>() ? in_step_tpb(g, (long long)g.nsys * g.nseg, kSmemThread)
+                                            : (g.tpb < kThomasThreads ? g.tpb : kThomasThreads);
+        const size_t smem = (size_t)tpb * kSmemThread;
+        if (smem > 48u * 1024u) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(k_modi_lu<Num, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
         dim3 grid(grid_x(g.nsys, tpb), (unsigned)g.nseg);
         k_modi_lu<Num, M><<<grid, tpb, smem, g.stream>>>(g);
     } else {

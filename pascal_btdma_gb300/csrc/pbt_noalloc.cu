@@ -141,6 +141,8 @@ extern "C" int pbt_solve_noncyclic_noalloc(double* a, double* b, double* c, doub
     g.nseg = nseg;
     g.tpb = pick_threads((long long)nsys * nseg, sms);
     g.stream = static_cast<cudaStream_t>(stream);
+    g.sms = sms;
+    g.tpb_auto = 1;
 
     cudaError_t e = cudaMemsetAsync(g.status, 0, sizeof(unsigned long long), g.stream);
     if (e == cudaSuccess) PBT_NOALLOC_DISPATCH(launch_modi)

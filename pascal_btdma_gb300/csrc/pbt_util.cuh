@@ -20,4 +20,11 @@ __device__ __forceinline__ size_t opaque(size_t v) {
 // constrains that.
 __device__ __forceinline__ void mem_fence_compiler() { asm volatile("" ::: "memory"); }
 
+// Barrier of the whole CTA for kernels whose warps go through the rows in
+// step.  The form without .aligned (sm_70 and later): the threads of one warp
+// may reach it from different instructions -- in a partial last CTA, the
+// threads without a system take the same number of barriers on a path of
+// their own -- and arrivals at barrier 0 count wherever they come from.
+__device__ __forceinline__ void cta_row_barrier() { asm volatile("barrier.sync 0;" ::: "memory"); }
+
 }  // namespace pbt

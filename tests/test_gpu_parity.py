@@ -291,6 +291,30 @@ def test_full_size_cyclic_against_oracle_subset(cuda, nseg, segmented):
         assert np.isfinite(D).all()
 
 
+@pytest.mark.parametrize("m,nsys,nrow,nseg,segmented,tpb", [
+    (5, 39999, 16, 1, False, 0),  # 250 CTAs of 160 threads, the last with 159 systems
+    (6, 39999, 12, 1, False, 0),
+    (5, 39999, 16, 4, True, 0),   # 179 x 4 CTAs of 224 threads, the last column with 127
+    (6, 20001, 12, 3, True, 0),   # 126 x 3 CTAs of 160 threads, the last column with 1
+    (5, 1000, 20, 1, False, 96),  # a CTA size fixed by the caller
+    (5, 1000, 20, 4, True, 96),
+])
+def test_ff_rows_in_step_partial_cta(cuda, m, nsys, nrow, nseg, segmented, tpb):
+    """The float-float split-row-step kernels keep a CTA's warps in step (a
+    barrier per row); the threads past the last system of a partial CTA take
+    the barriers only.  The systems of the partial CTA and a random sample
+    are checked against the oracle."""
+    w = synth.dominant(m, nsys, nrow, seed=77, delta=1.2)
+    rng = np.random.default_rng(3)
+    pick = np.unique(np.concatenate([np.arange(nsys - 40, nsys), rng.choice(nsys, size=40, replace=False)]))
+    ref = oracle_solve(subset(w, pick), nseg)
+    (_, _, _, D), singular = gpu_solve(w, nseg, precision="ff", reference_method=segmented, threads_per_block=tpb)
+    assert singular == 0
+    err = per_system_relerr(m, len(pick), nrow, column_subset(m, nsys, nrow, D, pick), ref.D)
+    assert err <= TOL_FF
+    assert np.isfinite(D).all()
+
+
 REFINE_TOL = 1e-10  # the mixed-precision target: FP32 factorisation + FP64 residual refinement
 
 
