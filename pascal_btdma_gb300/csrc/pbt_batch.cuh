@@ -79,8 +79,9 @@ __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTil
         if (!active) return;  // the lane rejoins at the next claim
         if constexpr (thomas_uses_lu<M>()) {
             // d solved apart: in this kernel, beside the local stage's
-            // body, the merged column loop raises the spills (cfg 3:
-            // float-float 17.90 vs 18.43 ms per sweep).
+            // body, the merged column loop raises the spills (uneven batch
+            // of 32768 systems, N 16..4096, m 2..5: float-float 17.90 vs
+            // 18.43 ms per sweep).
             thomas_body_lu<Num, M, false>(ba.a + mo, ba.b + mo, ba.c + mo, ba.d + vo, ba.cw + mo,
                                           batch_cps + threadIdx.x, blockDim.x, plane, rs, n_lane, true, bad);
         } else {
@@ -94,9 +95,9 @@ __device__ __forceinline__ void batch_stage1(const BatchArgs& ba, const BatchTil
         // Publish this segment; the warp completing the tile solves its
         // reduced system while the other warps go on with their items (no
         // warp waits: the update is the next launch).  Measured against a
-        // launch of its own, one warp per segmented tile (cfg 3, segments of
-        // 64 rows): float-float 17.94 vs 18.43 ms per sweep, FP64 24.60 vs
-        // 25.84 ms.
+        // launch of its own, one warp per segmented tile (the uneven batch
+        // above, segments of 64 rows): float-float 17.94 vs 18.43 ms per
+        // sweep, FP64 24.60 vs 25.84 ms.
         __threadfence();
         __syncwarp();
         int done = 0;

@@ -378,7 +378,7 @@ constexpr int kThomasThreads = PBT_THOMAS_THREADS;
 // Geometry of one solve as a body sees it: pointers already offset to the
 // thread's system (and segment), `plane` = element-plane stride, `rs` = row
 // stride (the number of systems interleaved in the layout).
-template <class Num, int M>
+template <class Num, int M, bool InStep = false>
 __device__ __forceinline__ void thomas_body(const double* A, const double* B, const double* C, double* D,
                                             double* CW, size_t plane0, size_t rs, int N, bool raw, unsigned& bad) {
     using T = typename Num::T;
@@ -386,6 +386,7 @@ __device__ __forceinline__ void thomas_body(const double* A, const double* B, co
     T cp[M][M], y[M];
     unsigned amax = 0;
     for (int q = 0; q < N; ++q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         const bool last = (q == N - 1);
@@ -439,6 +440,7 @@ PBT_UNROLL
         }
     }
     for (int q = N - 2; q >= 0; --q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         T c[M][M], t[M];
@@ -521,23 +523,58 @@ constexpr int kThomasLuMaxBlock = 6;
 // row (a barrier per row; InStep of thomas_body_lu / modi_body_lu).  Measured
 // on GB300 (m = 5): float-float issue is bound by instruction fetch, and
 // warps that run the same rows together share the instruction cache -- the
-// pencil batch (65536 x 256) 5.93 -> 5.37 ms in one segment, 18.7 -> 12.9 ms
-// in 16 (256-thread CTAs); the FP64 solve is bound by its pipe and gains
-// nothing (12.65 ms without, 14.09 ms with).
+// pencil batch (65536 x 256) 5.93 -> 5.46 ms in one segment, 18.7 -> 13.0 ms
+// in 16; the FP64 solve is bound by its pipe and gains nothing (12.65 ms
+// without, 14.09 ms with).
 template <class Num>
 __host__ __device__ constexpr bool rows_in_step() {
     return std::is_same<Num, FF>::value;
 }
+// Which kernels run in step, by measurement (float-float, GB300): the split
+// row step (m = 5, 6) and the periodic solve up to m = 6 (m = 5 pencil batch
+// of periodic lines 14.15 -> 12.09 ms); the fused forms up to m = 4, which
+// gain 1-2 % (m = 4: 65536 x 256 4.10 -> 4.01 ms, 256 lines of 32768 rows
+// in 128 segments 5.00 -> 4.94 ms).  From m = 7 on, where the fused forms keep
+// their blocks in local memory, the barrier costs 6-10 % (m = 8, 16384 x 256:
+// 57.5 -> 60.7 ms) and is left out, as in the adjoint (m = 4, 16384 lines
+// of 512 rows: 6.27 -> 6.85 ms with it).
+template <class Num, int M>
+__host__ __device__ constexpr bool fused_in_step() {
+    return rows_in_step<Num>() && M <= 4;
+}
+// The fused local stage also in FP32 (the refined solve's two-stage passes),
+// up to m = 6: pencil batch in 16 segments, refined, 18.14 -> 17.95 ms.
+template <class Num, int M>
+__host__ __device__ constexpr bool modi_in_step() {
+    return fused_in_step<Num, M>() || (std::is_same<Num, F32>::value && M <= 6);
+}
+template <class Num, int M>
+__host__ __device__ constexpr bool cyclic_in_step() {
+    return rows_in_step<Num>() && M <= 6;
+}
+
+// Registers a thread of kernel k takes (cudaFuncGetAttributes; 255 when the
+// query fails).
+template <class K>
+int kernel_regs(K* k) {
+    cudaFuncAttributes a{};
+    if (cudaFuncGetAttributes(&a, k) != cudaSuccess) {
+        cudaGetLastError();
+        return 255;
+    }
+    return a.numRegs > 0 ? a.numRegs : 255;
+}
 
 // CTA size of the in-step kernels: up to 256 threads, as many as two CTAs an
-// SM allow with `smem_thread` bytes of shared memory a thread, reduced so
+// SM allow with `smem_thread` bytes of shared memory and `regs` registers a
+// thread, reduced so
 // that `units` threads make whole waves of CTAs over the SMs (65536 systems
 // on 152 SMs: 224 threads, 293 CTAs, at most two an SM).  A CTA size fixed by
 // the caller (threads_per_block) is kept.
-inline int in_step_tpb(const SolveArgs& g, long long units, size_t smem_thread) {
+inline int in_step_tpb(const SolveArgs& g, long long units, size_t smem_thread, int regs) {
     if (!g.tpb_auto) return g.tpb;
     int cap = 256;
-    while (cap > 32 && 2 * ((size_t)cap * smem_thread + 1024) > 228u * 1024u) cap -= 32;
+    while (cap > 32 && (2 * ((size_t)cap * smem_thread + 1024) > 228u * 1024u || 2L * cap * regs > 65536L)) cap -= 32;
     const long long sms = g.sms > 0 ? g.sms : 1;
     const long long waves = (units + cap * sms - 1) / (cap * sms);
     long long tpb = (units + waves * sms - 1) / (waves * sms);
@@ -791,16 +828,21 @@ PBT_UNROLL
 }
 
 
-// The barriers of thomas_body_lu<..., InStep = true> for a thread without a
-// system: the same loop headers, one barrier per forward and backward row.
-__device__ __forceinline__ void thomas_idle_rows(int N) {
+template <class Num, int M>
+__host__ __device__ constexpr bool thomas_in_step() {
+    return thomas_uses_lu<M>() ? rows_in_step<Num>() : fused_in_step<Num, M>();
+}
+// The barriers of thomas_body_lu / thomas_body <..., InStep = true> for a
+// thread without a system: the same loop headers, one barrier per forward and
+// backward row.
+static __device__ __noinline__ void thomas_idle_rows(int N) {
     for (int q = 0; q < N; ++q) cta_row_barrier();
     for (int q = N - 2; q >= 0; --q) cta_row_barrier();
 }
 
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
-    constexpr bool kStep = thomas_uses_lu<M>() && rows_in_step<Num>();
+    constexpr bool kStep = thomas_in_step<Num, M>();
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
     if (sys >= g.nsys) {
         if constexpr (kStep) thomas_idle_rows(g.nrow);
@@ -813,7 +855,7 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
             g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, thomas_cps + threadIdx.x, blockDim.x,
             (size_t)g.nsys * g.nrow, (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
     } else {
-        thomas_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
+        thomas_body<Num, M, kStep>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, (size_t)g.nsys * g.nrow,
                             (size_t)g.nsys, g.nrow, g.factors_raw != 0, bad);
     }
     report_status(g.status, bad);
@@ -886,7 +928,7 @@ __host__ __device__ constexpr int cyclic_slots() {
     return 2 * M * M + M;
 }
 
-template <class Num, int M>
+template <class Num, int M, bool InStep = false>
 __device__ __forceinline__ void thomas_cyclic_body(const double* A, const double* B, const double* C, double* D,
                                                    double* CW, double* EW, double* cps, int cstride, size_t plane0,
                                                    size_t rs, int N, bool raw, unsigned& bad) {
@@ -903,6 +945,7 @@ __device__ __forceinline__ void thomas_cyclic_body(const double* A, const double
     auto slot = [&](int s) -> double* { return cps + s * cstride; };
     T y[M];
     for (int q = 1; q < N; ++q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const bool last = (q == N - 1);
         // W = A_q e'_{q-1} into the e slots; row 1: W = A_1 (its e is -A_1).
@@ -1055,6 +1098,7 @@ PBT_UNROLL
 PBT_UNROLL
     for (int k = 0; k < M; ++k) Num::sts(slot(kY + k), y[k]);
     for (int q = N - 2; q >= 1; --q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         T c[M][M], t[M];
@@ -1158,6 +1202,7 @@ PBT_UNROLL
         out_vec<Num, M>(D, opaque(plane0), x0, amax);
     }
     for (int q = 1; q < N; ++q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         T e[M][M], t[M];
@@ -1175,13 +1220,25 @@ PBT_UNROLL
     bad |= range_bits<Num>(amax, true);
 }
 
+// The barriers of thomas_cyclic_body<..., InStep = true> for a thread
+// without a system: the same loop headers (forward, backward, solution).
+static __device__ __noinline__ void cyclic_idle_rows(int N) {
+    for (int q = 1; q < N; ++q) cta_row_barrier();
+    for (int q = N - 2; q >= 1; --q) cta_row_barrier();
+    for (int q = 1; q < N; ++q) cta_row_barrier();
+}
+
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_cyclic(const SolveArgs g) {
+    constexpr bool kStep = cyclic_in_step<Num, M>();
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
+    if (sys >= g.nsys) {
+        if constexpr (kStep) cyclic_idle_rows(g.nrow);
+        return;
+    }
     extern __shared__ double thomas_cps[];
     unsigned bad = 0;
-    thomas_cyclic_body<Num, M>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, g.re + sys,
+    thomas_cyclic_body<Num, M, kStep>(g.a + sys, g.b + sys, g.c + sys, g.d + sys, g.cw + sys, g.re + sys,
                                thomas_cps + threadIdx.x, blockDim.x, (size_t)g.nsys * g.nrow, (size_t)g.nsys,
                                g.nrow, g.factors_raw != 0, bad);
     report_status(g.status, bad);
@@ -1192,7 +1249,7 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_cyclic(const SolveArgs 
 // ---------------------------------------------------------------------------
 // A..CW point at the segment's first row of this system; RA..RD at this
 // system in the reduced layout (row stride rrs, plane stride rplane).
-template <class Num, int M>
+template <class Num, int M, bool InStep = false>
 __device__ __forceinline__ void modi_body(const double* A, const double* B, const double* C, double* D, double* AW,
                                           double* CW, size_t plane0, size_t rs, int n, bool raw, double* RA,
                                           double* RC, double* RD, size_t rplane, size_t rrs, int seg, unsigned& bad) {
@@ -1203,6 +1260,7 @@ __device__ __forceinline__ void modi_body(const double* A, const double* B, cons
     // Rows 1 and 2 of the segment: [A'|C'|d'] = B^{-1}[A|C|d]; rows 3..n:
     // R = B - A C'_{q-1}; [A'|C'|d'] = R^{-1}[-A A'_{q-1} | C | d - A d'_{q-1}].
     for (int q = 0; q < n; ++q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         const bool first2 = (q < 2);
@@ -1270,6 +1328,7 @@ PBT_UNROLL
         ld_raw_vec<Num, M>(dp, D + o1, plane0);
     }
     for (int q = n - 3; q >= 1; --q) {
+        if constexpr (InStep) cta_row_barrier();
         const size_t o = (size_t)q * rs;
         const size_t plane = opaque(plane0);
         T a[M][M], c[M][M], dq[M];
@@ -1672,7 +1731,7 @@ PBT_UNROLL
 
 // The barriers of modi_body_lu<..., InStep = true> for a thread without a
 // system: the same loop headers, one barrier per forward and backward row.
-__device__ __forceinline__ void modi_idle_rows(int n) {
+static __device__ __noinline__ void modi_idle_rows(int n) {
     for (int q = 0; q < n; ++q) cta_row_barrier();
     for (int q = n - 3; q >= 1; --q) cta_row_barrier();
 }
@@ -1700,16 +1759,20 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_modi_lu(const SolveArgs g) {
 }
 
 template <class Num, int M>
-__global__ void __launch_bounds__(128) k_modi(const SolveArgs g) {
+__global__ void __launch_bounds__(256) k_modi(const SolveArgs g) {
+    constexpr bool kStep = modi_in_step<Num, M>();
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
     const int seg = blockIdx.y;
     int f, l;
     seg_rows(g.nrow, g.nseg, seg, f, l);
+    if (sys >= g.nsys) {
+        if constexpr (kStep) modi_idle_rows(l - f + 1);
+        return;
+    }
     const size_t rs = (size_t)g.nsys;
     const size_t fo = (size_t)f * rs + sys;
     unsigned bad = 0;
-    modi_body<Num, M>(g.a + fo, g.b + fo, g.c + fo, g.d + fo, g.aw + fo, g.cw + fo, rs * g.nrow, rs, l - f + 1,
+    modi_body<Num, M, kStep>(g.a + fo, g.b + fo, g.c + fo, g.d + fo, g.aw + fo, g.cw + fo, rs * g.nrow, rs, l - f + 1,
                       g.factors_raw != 0, g.ra + sys, g.rc + sys, g.rd + sys, rs * 2 * g.nseg, rs, seg, bad);
     report_status(g.status, bad);
 }
@@ -2576,9 +2639,11 @@ inline unsigned grid_x(int nsys, int tpb) { return (unsigned)((nsys + tpb - 1) /
 
 template <class Num, int M>
 cudaError_t launch_thomas(const SolveArgs& g) {
-    constexpr bool kStep = thomas_uses_lu<M>() && rows_in_step<Num>();
+    constexpr bool kStep = thomas_in_step<Num, M>();
     constexpr size_t kSmemThread = thomas_uses_lu<M>() ? (M * M + M) * sizeof(double) : 0;
-    const int tpb = kStep ? in_step_tpb(g, g.nsys, kSmemThread) : (g.tpb < kThomasThreads ? g.tpb : kThomasThreads);
+    static const int regs = kernel_regs(k_thomas<Num, M>);
+    const int tpb =
+        kStep ? in_step_tpb(g, g.nsys, kSmemThread, regs) : (g.tpb < kThomasThreads ? g.tpb : kThomasThreads);
     const size_t smem = (size_t)tpb * kSmemThread;
     if (smem > 48u * 1024u) {
         const cudaError_t e =
@@ -2608,6 +2673,10 @@ cudaError_t launch_thomas_cyclic(const SolveArgs& g) {
     } else {
         int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
         if (M > 6) tpb = 32;
+        if (cyclic_in_step<Num, M>()) {
+            static const int regs = kernel_regs(k_thomas_cyclic<Num, M>);
+            tpb = in_step_tpb(g, g.nsys, cyclic_slots<Num, M>() * sizeof(double), regs);
+        }
         const size_t smem = (size_t)tpb * cyclic_slots<Num, M>() * sizeof(double);
         if (smem > 48u * 1024u) {
             const cudaError_t e = cudaFuncSetAttribute(k_thomas_cyclic<Num, M>,
@@ -2622,7 +2691,8 @@ template <class Num, int M>
 cudaError_t launch_modi(const SolveArgs& g) {
     if constexpr (modi_uses_lu<Num, M>()) {
         constexpr size_t kSmemThread = cyclic_slots<Num, M>() * sizeof(double);
-        const int tpb = rows_in_step<Num>() ? in_step_tpb(g, (long long)g.nsys * g.nseg, kSmemThread)
+        static const int regs = kernel_regs(k_modi_lu<Num, M>);
+        const int tpb = rows_in_step<Num>() ? in_step_tpb(g, (long long)g.nsys * g.nseg, kSmemThread, regs)
                                             : (g.tpb < kThomasThreads ? g.tpb : kThomasThreads);
         const size_t smem = (size_t)tpb * kSmemThread;
         if (smem > 48u * 1024u) {
@@ -2633,8 +2703,10 @@ cudaError_t launch_modi(const SolveArgs& g) {
         dim3 grid(grid_x(g.nsys, tpb), (unsigned)g.nseg);
         k_modi_lu<Num, M><<<grid, tpb, smem, g.stream>>>(g);
     } else {
-        dim3 grid(grid_x(g.nsys, g.tpb), (unsigned)g.nseg);
-        k_modi<Num, M><<<grid, g.tpb, 0, g.stream>>>(g);
+        static const int regs = kernel_regs(k_modi<Num, M>);
+        const int tpb = modi_in_step<Num, M>() ? in_step_tpb(g, (long long)g.nsys * g.nseg, 0, regs) : g.tpb;
+        dim3 grid(grid_x(g.nsys, tpb), (unsigned)g.nseg);
+        k_modi<Num, M><<<grid, tpb, 0, g.stream>>>(g);
     }
     return cudaGetLastError();
 }

@@ -291,27 +291,33 @@ def test_full_size_cyclic_against_oracle_subset(cuda, nseg, segmented):
         assert np.isfinite(D).all()
 
 
-@pytest.mark.parametrize("m,nsys,nrow,nseg,segmented,tpb", [
-    (5, 39999, 16, 1, False, 0),  # 250 CTAs of 160 threads, the last with 159 systems
-    (6, 39999, 12, 1, False, 0),
-    (5, 39999, 16, 4, True, 0),   # 179 x 4 CTAs of 224 threads, the last column with 127
-    (6, 20001, 12, 3, True, 0),   # 126 x 3 CTAs of 160 threads, the last column with 1
-    (5, 1000, 20, 1, False, 96),  # a CTA size fixed by the caller
-    (5, 1000, 20, 4, True, 96),
+@pytest.mark.parametrize("m,nsys,nrow,nseg,segmented,tpb,cyclic,prec", [
+    (5, 39999, 16, 1, False, 0, False, "ff"),  # 250 CTAs of 160 threads, the last with 159 systems
+    (6, 39999, 12, 1, False, 0, False, "ff"),
+    (5, 39999, 16, 4, True, 0, False, "ff"),   # 179 x 4 CTAs of 224 threads, the last column with 127
+    (6, 20001, 12, 3, True, 0, False, "ff"),   # 126 x 3 CTAs of 160 threads, the last column with 1
+    (5, 1000, 20, 1, False, 96, False, "ff"),  # a CTA size fixed by the caller
+    (5, 1000, 20, 4, True, 96, False, "ff"),
+    (3, 39999, 16, 1, False, 0, False, "ff"),  # the fused forms, m <= 4
+    (4, 39999, 16, 4, True, 0, False, "ff"),
+    (5, 39999, 12, 1, False, 0, True, "ff"),   # the periodic solve
+    (2, 39999, 9, 1, False, 0, True, "ff"),
+    (5, 39999, 16, 4, True, 0, False, "fp32_refine"),  # the FP32 local stage of the refined solve
 ])
-def test_ff_rows_in_step_partial_cta(cuda, m, nsys, nrow, nseg, segmented, tpb):
-    """The float-float split-row-step kernels keep a CTA's warps in step (a
-    barrier per row); the threads past the last system of a partial CTA take
-    the barriers only.  The systems of the partial CTA and a random sample
-    are checked against the oracle."""
-    w = synth.dominant(m, nsys, nrow, seed=77, delta=1.2)
+def test_rows_in_step_partial_cta(cuda, m, nsys, nrow, nseg, segmented, tpb, cyclic, prec):
+    """The kernels that keep a CTA's warps in step (a barrier per row): the
+    threads past the last system of a partial CTA take the barriers only.
+    The systems of the partial CTA and a random sample are checked against
+    the oracle."""
+    w = synth.fill(synth.DOMINANT, m, nsys, nrow, seed=77, delta=1.2, flags=0 if cyclic else synth.ZERO_ENDS)
     rng = np.random.default_rng(3)
     pick = np.unique(np.concatenate([np.arange(nsys - 40, nsys), rng.choice(nsys, size=40, replace=False)]))
-    ref = oracle_solve(subset(w, pick), nseg)
-    (_, _, _, D), singular = gpu_solve(w, nseg, precision="ff", reference_method=segmented, threads_per_block=tpb)
+    ref = oracle_solve(subset(w, pick), nseg, cyclic=cyclic)
+    (_, _, _, D), singular = gpu_solve(w, nseg, cyclic=cyclic, precision=prec, reference_method=segmented,
+                                       threads_per_block=tpb)
     assert singular == 0
     err = per_system_relerr(m, len(pick), nrow, column_subset(m, nsys, nrow, D, pick), ref.D)
-    assert err <= TOL_FF
+    assert err <= (REFINE_TOL if prec == "fp32_refine" else TOL_FF)
     assert np.isfinite(D).all()
 
 
