@@ -868,16 +868,20 @@ __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas(const SolveArgs g) {
 // slower.
 template <class Num, int M>
 __global__ void __maxnreg__(PBT_THOMAS_MAXNREG) k_thomas_lines(const SolveArgs g, const LineStrides ls) {
+    constexpr bool kStep = thomas_in_step<Num, M>();
     const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= g.nsys) return;
+    if (sys >= g.nsys) {
+        if constexpr (kStep) thomas_idle_rows(g.nrow);
+        return;
+    }
     unsigned bad = 0;
     const size_t o = (size_t)(sys % ls.lin) * (size_t)ls.in + (size_t)(sys / ls.lin) * (size_t)ls.out;
     if constexpr (thomas_uses_lu<M>()) {
         extern __shared__ double thomas_cps[];
-        thomas_body_lu<Num, M>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, thomas_cps + threadIdx.x, blockDim.x,
+        thomas_body_lu<Num, M, (PBT_LU_MERGE_Y != 0), kStep>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, thomas_cps + threadIdx.x, blockDim.x,
                                (size_t)ls.elem, (size_t)ls.row, g.nrow, g.factors_raw != 0, bad);
     } else {
-        thomas_body<Num, M>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, (size_t)ls.elem, (size_t)ls.row, g.nrow,
+        thomas_body<Num, M, kStep>(g.a + o, g.b + o, g.c + o, g.d + o, g.cw + o, (size_t)ls.elem, (size_t)ls.row, g.nrow,
                             g.factors_raw != 0, bad);
     }
     report_status(g.status, bad);
@@ -2658,8 +2662,16 @@ cudaError_t launch_thomas_lines(const SolveArgs& g, const LineStrides& ls) {
     if constexpr (std::is_same<Num, F32>::value) {
         return cudaErrorInvalidValue;  // FP64 and float-float plans only
     } else {
-        const int tpb = g.tpb < kThomasThreads ? g.tpb : kThomasThreads;
-        const size_t smem = thomas_uses_lu<M>() ? (size_t)tpb * (M * M + M) * sizeof(double) : 0;
+        constexpr size_t kSmemThread = thomas_uses_lu<M>() ? (M * M + M) * sizeof(double) : 0;
+        static const int regs = kernel_regs(k_thomas_lines<Num, M>);
+        const int tpb = thomas_in_step<Num, M>() ? in_step_tpb(g, g.nsys, kSmemThread, regs)
+                                                 : (g.tpb < kThomasThreads ? g.tpb : kThomasThreads);
+        const size_t smem = (size_t)tpb * kSmemThread;
+        if (smem > 48u * 1024u) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(k_thomas_lines<Num, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
         k_thomas_lines<Num, M><<<grid_x(g.nsys, tpb), tpb, smem, g.stream>>>(g, ls);
         return cudaGetLastError();
     }
