@@ -169,7 +169,11 @@ int pbt_plan_destroy(pbt_plan* plan);
 /* Replaces solve_noncyclic (pascal_btdma_cuda.cu:1035-1045, impl :853-908)
  * and btdma_many_mpi_gpu_v2 (mod_btdma_gpu_v2.f90:131-167).  m, nsys, nrow
  * must equal the plan's (PBT_EINVAL otherwise, like the reference's check at
- * pascal_btdma_cuda.cu:868-870). */
+ * pascal_btdma_cuda.cu:868-870).
+ * Graph capture: the first solve of a kind (block size, arithmetic, method)
+ * on a device loads its kernels there and sets their launch attributes
+ * (register count query, shared-memory size); make one such solve before
+ * capturing solves in a CUDA graph. */
 int pbt_solve_noncyclic(pbt_plan* plan, double* a, double* b, double* c, double* d,
                         int m, int nsys, int nrow, void* stream);
 
