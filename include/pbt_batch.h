@@ -25,8 +25,10 @@
  * Tuning (pbt_batch_tuning): the number of segments of each tile is
  * round(N_max / seg_len[m]) (one segment when seg_len[m] <= 0), so long lines
  * use the two-stage method and no single warp's chain of rows dominates the
- * launch; warps_per_cta sets the persistent CTA size.  An autotuner picks
- * these per (m, N, nsys) bucket (pascal_btdma_gb300/batch.py).
+ * launch; warps_per_cta sets the persistent CTA size (float-float m = 5, 6,
+ * whose local stage keeps a CTA's warps on the same row, always runs 8-warp
+ * CTAs there).  An autotuner picks these per (m, N, nsys) bucket
+ * (pascal_btdma_gb300/batch.py).
  */
 #ifndef PBT_BATCH_H
 #define PBT_BATCH_H
