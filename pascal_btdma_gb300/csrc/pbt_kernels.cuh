@@ -355,9 +355,10 @@ PBT_UNROLL
 // [C'_q | y_q] = R_q^{-1} [C_q | d_q - A_q y_{q-1}]; C' goes to cw, y to D.
 // Backward: x_q = y_q - C'_q x_{q+1}.
 // ---------------------------------------------------------------------------
-// Launch shape of k_thomas: 64-thread CTAs, at most 128 registers per
-// thread, i.e. 16 warps per SM, so the 2048 warps of a 65536-system batch run
-// in one wave.  The kernel is bound by memory latency at m = 5 (one thread
+// Launch shape of k_thomas: at most 128 registers per thread, i.e. 16 warps
+// per SM, so the 2048 warps of a 65536-system batch run in one wave; 64-thread
+// CTAs where the rows are not in step (FP64, FP32), in_step_tpb's CTAs (up
+// to 256 threads) where they are (float-float).  The kernel is bound by memory latency at m = 5 (one thread
 // carries a whole block row), so resident warps matter more than the few
 // spills the cap causes: on GB300 the float-float m = 5 solve runs in 8.3 ms
 // at 128 registers, 9.8 ms at 168 (a second, latency-bound wave) and 9.7 ms at
