@@ -123,7 +123,9 @@ typedef struct pbt_plan_desc {
     unsigned flags;        /* PBT_FLAG_* */
     double tol;            /* PBT_PREC_FP32_REFINE: target relative correction size */
     int max_iter;          /* PBT_PREC_FP32_REFINE: refinement iteration cap */
-    int threads_per_block; /* 0 = choose automatically */
+    int threads_per_block; /* 0 = choose automatically (float-float kernels whose
+                              CTAs keep their warps on the same row take up to 256
+                              threads); else a multiple of 32 in 32..128, used as is */
     int reserved[7];
 } pbt_plan_desc;
 
